@@ -1,0 +1,364 @@
+"""Benchmark: particle pushes per second of the full PIC step on one GB300.
+
+Workload (the reference's throughput configuration): uniform thermal plasma,
+128^3 periodic cells, 64 electrons per cell (134,217,728 particles), FP32,
+u_th = 0.05, dt = 0.7 Courant, zero initial fields, particles re-sorted by
+cell every 20 steps.  A "step" is the reference's whole time step
+(example/example.cpp:221-271): interpolator load, accumulator clear, push with
+deposit, accumulator unload, B half step, E step, B half step, field energies,
+plus the amortised sort.  The particle list (4.3 GB) is larger than L2, so no
+L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is pushes/s with the state resident in HBM;
+`e2e` is the same metric through the public API with the initial state copied
+from pinned host memory and the final state copied back inside the timed
+region (plus each step's energies read back); `roofline` covers the push
+kernel; `cpu_baseline` is the CPU restatement (OpenMP, all host cores) on a
+bounded sample of the same workload.  `--impl reference` times that CPU
+implementation as the reference arm (the reference itself needs Kokkos and
+Cabana, which are not available to build).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SORT_INTERVAL = 20
+N_CELLS = 128
+PPC = 64
+# algorithmic bytes of push+deposit: per particle read 7 reals + cell, write 6
+# reals; per interior cell the 18 interpolator coefficients and 12 accumulators
+BYTES_PER_PARTICLE = {4: 56, 8: 108}
+BYTES_PER_CELL = {4: 120, 8: 240}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic_from_profiles():
+    """DRAM bytes per push launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "push_thermal128_fp32.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_full_launch:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        import tempfile
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        cmd = ["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits", "-lms", "200"]
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].strip()
+        if vis:
+            cmd += ["-i", vis]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- GPU arm
+def gpu_run(precision, steps, warmup, ws, host_packed=None):
+    """Device-resident timed loop; returns dict with times and push events."""
+    import torch
+    from cabanapic_gb300 import decks
+    from cabanapic_gb300.simulation import Simulation
+
+    deck = decks.thermal(n=N_CELLS, ppc=PPC, precision=precision, num_steps=steps + warmup)
+    if host_packed is None:
+        host_packed = decks.thermal_particles(deck, packed=True)
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        sim.step()
+    torch.cuda.synchronize()
+    _barrier(ws)
+    sim.time_push = True
+    sim.push_events = []
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        sim.step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    push_ms = sim.push_times_ms()
+    sim.check_status()
+    res = dict(ms=ms, push_ms=push_ms, deck=deck, energies=sim.energies())
+    del sim
+    torch.cuda.empty_cache()
+    return res, host_packed
+
+
+def e2e_run(precision, steps, warmup, host_packed, ws):
+    """Same step loop through the public API, with host buffers: the initial
+    particle state is copied from pinned host memory, each step's energies are
+    read back to pinned host memory, and the final particle state is copied
+    back, all inside the timed region."""
+    import torch
+    from cabanapic_gb300 import decks, pic
+    from cabanapic_gb300.simulation import Simulation
+
+    deck = decks.thermal(n=N_CELLS, ppc=PPC, precision=precision, num_steps=steps + warmup)
+    pinned_in = torch.from_numpy(host_packed).pin_memory()
+    pinned_out = torch.empty_like(pinned_in).pin_memory()
+    energies_host = torch.empty((steps, 2), dtype=torch.float64).pin_memory()
+    # warm-up on the same arrays (not timed), then reset the state from the host
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup)
+    for _ in range(warmup):
+        sim.step()
+    torch.cuda.synchronize()
+    sim.step_no = 0
+    stream = torch.cuda.current_stream()
+    _barrier(ws)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.particles.buf[: sim.particles.nbytes].copy_(pinned_in, non_blocking=True)
+    sim.fields.buf.zero_()
+    for k in range(steps):
+        sim.step()
+        energies_host[k].copy_(sim.energy[k], non_blocking=True)
+    pinned_out.copy_(sim.particles.buf[: sim.particles.nbytes], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    pic.check_status()
+    h2d = host_packed.nbytes
+    d2h = host_packed.nbytes + steps * 16
+    del sim
+    torch.cuda.empty_cache()
+    return dict(ms=ms, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps)
+
+
+# ---------------------------------------------------------------- CPU (oracle) arm
+def cpu_sample_run(steps, warmup, precision=4, sample_ppc=8, threads=0):
+    """The CPU restatement (OpenMP push with per-thread accumulator copies,
+    field phase in C++) on the 128^3 grid with `sample_ppc` particles per cell;
+    returns (pushes/s, threads, particles)."""
+    import oracle
+    from cabanapic_gb300 import decks, layout as L
+
+    orc = oracle.load()
+    deck = decks.thermal(n=N_CELLS, ppc=sample_ppc, precision=precision)
+    p = deck.derived()
+    R = deck.R
+    buf = decks.thermal_particles(deck, packed=True)
+    nc = deck.num_cells
+    g = orc.grid(deck.nx, deck.ny, deck.nz)
+    fields = np.zeros(L.cell_array_bytes(nc, 9, R) // np.dtype(R).itemsize, R)
+    interp = np.zeros(L.cell_array_bytes(nc, 18, R) // np.dtype(R).itemsize, R)
+    acc = np.zeros((nc, 3, 4), R)
+    n = deck.num_particles
+    h = R(0.5)
+    used = 1
+
+    def one_step():
+        nonlocal used
+        orc.load_interpolator(fields, interp, g)
+        acc.fill(0)
+        used = orc.push_omp(buf, n, 32, interp, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
+                            p["qsp"], acc, g, threads)
+        orc.unload_accumulator(fields, acc, g, p["dx"], p["dy"], p["dz"], p["dt"])
+        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
+        orc.advance_e(fields, p["px"], p["py"], p["pz"], g, p["dt_eps0"])
+        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
+        orc.energies(fields, g)
+
+    for _ in range(warmup):
+        one_step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one_step()
+    dt = time.perf_counter() - t0
+    return n * steps / dt, used, n, dt
+
+
+# ---------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    metric = "particle-pushes/s (full step, thermal plasma 128^3 x 64 ppc)"
+    unit = "particle-pushes/s"
+    workload = ("thermal plasma 128^3 cells x 64 ppc = 134,217,728 particles, FP32, u_th=0.05, "
+                "dt=0.7 Courant, sort every 20 steps; full step (interp, clear, push+deposit, "
+                "unload, advance_b/e/b, energies)")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(1, min(args.steps, 5))
+        warm = max(1, min(args.warmup, 1))
+        v, cores, n, secs = cpu_sample_run(steps, warm)
+        sample = (f"128^3 grid, 8 ppc ({n:,} particles), {steps} timed steps after {warm}; "
+                  "CPU restatement of the reference (OpenMP push, per-thread accumulators)")
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": args.gpus,
+                "steps": steps, "warmup": warm, "ms_per_step": secs / steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": {"workload": workload, "sample": sample},
+                "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+                "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from cabanapic_gb300 import capi
+    capi.load()
+
+    sampler = ClockSampler()
+    sampler.start()
+    res, host_packed = gpu_run(4, args.steps, max(args.warmup, 3), ws)
+    clocks = sampler.stop()
+    deck = res["deck"]
+    n = deck.num_particles
+    ms = _barrier_max(res["ms"], ws)
+    value = n * args.steps * ws / (ms / 1e3)
+    push_ms = float(np.mean(res["push_ms"]))
+    alg_bytes = n * BYTES_PER_PARTICLE[4] + deck.num_interior * BYTES_PER_CELL[4]
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / (push_ms / 1e3) / 1e9
+    traffic = _traffic_from_profiles()
+    per_step_launches = 11  # interp, push, unload, 2x(advance_b + ghost copy), fold, ghost copy, advance_e, energies
+    launches = args.steps * per_step_launches + 6 * len(range(0, args.steps, SORT_INTERVAL))
+
+    e2e = None
+    if not args.no_e2e:
+        r = e2e_run(4, args.steps, max(args.warmup, 3), host_packed, ws)
+        ems = _barrier_max(r["ms"], ws)
+        e2e = {"value": n * args.steps * ws / (ems / 1e3), "unit": unit,
+               "h2d_bytes_per_step": int(r["h2d_per_step"]), "d2h_bytes_per_step": int(r["d2h_per_step"]),
+               "ms_per_step": ems / args.steps}
+    del host_packed
+
+    fp64 = None
+    if not args.no_fp64:
+        k64 = max(2, min(args.steps, 10))
+        r64, hp = gpu_run(8, k64, 3, ws)
+        del hp
+        ms64 = _barrier_max(r64["ms"], ws)
+        p64 = float(np.mean(r64["push_ms"]))
+        fp64 = {"value": n * k64 * ws / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
+                "push_ms": p64, "fp32_over_fp64": (value / (n * k64 * ws / (ms64 / 1e3)))}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, cores, ns, secs = cpu_sample_run(3, 1)
+        cpu = {"value": v, "unit": unit, "cores": cores, "kind": "port",
+               "sample": f"128^3 grid, 8 ppc ({ns:,} particles), 3 full steps after 1 ({secs:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": metric, "value": value, "unit": unit, "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "particles": n, "cells": deck.num_cells,
+                       "l2": "particle list 4.3 GB > L2: no flush needed", "replicas": ws},
+            "push_ms": push_ms,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "fp64": fp64,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+"""Device containers with the reference's layouts.
+
+Stand-ins for the reference's Cabana/Kokkos containers (src/types.h):
+ParticleList ~ particle_list_t, InterpolatorArray ~ interpolator_array_t,
+AccumulatorArray ~ accumulator_array_t, FieldArray ~ field_array_t.  Device
+memory comes from torch (the plumbing); the kernels see raw pointers through
+the C ABI.  Layout conversion to and from host arrays is in layout.py.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import layout as L
+
+
+def _dev(device):
+    return torch.device(device if device is not None else "cuda")
+
+
+def _torch_real(real: np.dtype):
+    return torch.float32 if np.dtype(real) == np.float32 else torch.float64
+
+
+class ParticleList:
+    """particle_list_t: Cabana AoSoA<real_t x7, int> of n particles."""
+
+    def __init__(self, n: int, real=np.float32, vl: int = 32, device=None):
+        self.n = int(n)
+        self.real = np.dtype(real)
+        self.vl = int(vl)
+        self.nbytes = L.particle_list_bytes(self.n, self.real, self.vl)
+        self.buf = torch.zeros(max(self.nbytes, 16), dtype=torch.uint8, device=_dev(device))
+
+    @property
+    def precision(self) -> int:
+        return self.real.itemsize
+
+    @property
+    def ptr(self) -> int:
+        return self.buf.data_ptr()
+
+    def size(self) -> int:
+        return self.n
+
+    def upload(self, host) -> "ParticleList":
+        """host: dict of member arrays or packed AoSoA bytes."""
+        packed = host if isinstance(host, np.ndarray) else L.pack_particles(host, self.real, self.vl)
+        assert packed.nbytes == self.nbytes, (packed.nbytes, self.nbytes)
+        self.buf[: self.nbytes].copy_(torch.from_numpy(packed.view(np.uint8)))
+        return self
+
+    def download_bytes(self) -> np.ndarray:
+        return self.buf[: self.nbytes].cpu().numpy()
+
+    def download(self) -> dict:
+        return L.unpack_particles(self.download_bytes(), self.n, self.real, self.vl)
+
+
+class _CellArray:
+    members = 0
+
+    def __init__(self, num_cells: int, real=np.float32, device=None):
+        self.num_cells = int(num_cells)
+        self.real = np.dtype(real)
+        n = L.cell_array_bytes(self.num_cells, self.members, self.real) // self.real.itemsize
+        self.buf = torch.zeros(n, dtype=_torch_real(self.real), device=_dev(device))
+
+    @property
+    def precision(self) -> int:
+        return self.real.itemsize
+
+    @property
+    def ptr(self) -> int:
+        return self.buf.data_ptr()
+
+    def size(self) -> int:
+        return self.num_cells
+
+    def set_members(self, vals: np.ndarray) -> None:
+        """vals: (num_cells, members) host array."""
+        self.buf.copy_(torch.from_numpy(L.pack_cells(np.asarray(vals), self.real)))
+
+    def get_members(self) -> np.ndarray:
+        return L.unpack_cells(self.buf.cpu().numpy(), self.num_cells, self.members)
+
+
+class InterpolatorArray(_CellArray):
+    """interpolator_array_t: AoSoA of 18 coefficients per cell, 32-cell blocks."""
+    members = L.INTERP_MEMBERS
+
+
+class FieldArray(_CellArray):
+    """field_array_t: AoSoA of ex ey ez cbx cby cbz jfx jfy jfz, 32-cell blocks."""
+    members = L.FIELD_MEMBERS
+
+
+class AccumulatorArray:
+    """accumulator_array_t: View<real_t*[3][4]> in LayoutRight."""
+
+    def __init__(self, num_cells: int, real=np.float32, device=None):
+        self.num_cells = int(num_cells)
+        self.real = np.dtype(real)
+        self.buf = torch.zeros((self.num_cells, 3, 4), dtype=_torch_real(self.real), device=_dev(device))
+
+    @property
+    def precision(self) -> int:
+        return self.real.itemsize
+
+    @property
+    def ptr(self) -> int:
+        return self.buf.data_ptr()
+
+    def size(self) -> int:
+        return self.num_cells
+
+    def get(self) -> np.ndarray:
+        return self.buf.cpu().numpy()
+
+    def set(self, vals: np.ndarray) -> None:
+        self.buf.copy_(torch.from_numpy(np.asarray(vals, self.real).reshape(self.num_cells, 3, 4)))

@@ -1,0 +1,75 @@
+// common.cuh -- device-side layout access and launch helpers shared by the
+// hot-path kernels.  Layouts are the reference's (include/cpic/layout.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cpic/capi.h"
+
+namespace cpic {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kCellBlock = CPIC_CELL_BLOCK;
+
+// Ghosted grid extents and VOXEL (src/types.h:195).
+struct GridDev {
+  int nx, ny, nz;   // interior cells
+  int sx, sy, sz;   // ghosted extents (n + 2)
+  int num_cells;    // sx * sy * sz
+  __host__ __device__ int vox(int x, int y, int z) const { return x + sx * (y + sy * z); }
+};
+
+inline GridDev make_grid(const cpic_grid* g) {
+  GridDev d;
+  d.nx = (int)g->nx; d.ny = (int)g->ny; d.nz = (int)g->nz;
+  d.sx = d.nx + 2; d.sy = d.ny + 2; d.sz = d.nz + 2;
+  d.num_cells = d.sx * d.sy * d.sz;
+  return d;
+}
+
+// Member m of cell c in a cell AoSoA with NM members (interpolator 18, field 9).
+template <int NM>
+__host__ __device__ __forceinline__ size_t cell_at(int c, int m) {
+  return (size_t)(c >> 5) * (NM * kCellBlock) + (size_t)m * kCellBlock + (c & 31);
+}
+
+// Particle AoSoA of vector length VL: byte offset of member m (0..6 real, 7 cell) of particle p.
+template <class R, int VL>
+struct PLayout {
+  static constexpr size_t kBlock = (size_t)VL * (7 * sizeof(R) + sizeof(int));
+  __device__ __forceinline__ static size_t off(int64_t p, int m) {
+    return (size_t)(p / VL) * kBlock + (size_t)m * VL * sizeof(R) + (size_t)(p % VL) * sizeof(R);
+  }
+  __device__ __forceinline__ static size_t cell_off(int64_t p) {
+    return (size_t)(p / VL) * kBlock + (size_t)7 * VL * sizeof(R) + (size_t)(p % VL) * sizeof(int);
+  }
+};
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ void red_add(float* a, float v) { atomicAdd(a, v); }
+__device__ __forceinline__ void red_add(double* a, double v) { atomicAdd(a, v); }
+
+// Four consecutive accumulator values (16-byte aligned) in one vector reduction.
+__device__ __forceinline__ void red_add4(float* a, float v0, float v1, float v2, float v3) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(a), "f"(v0), "f"(v1), "f"(v2),
+               "f"(v3)
+               : "memory");
+}
+__device__ __forceinline__ void red_add4(double* a, double v0, double v1, double v2, double v3) {
+  atomicAdd(a + 0, v0); atomicAdd(a + 1, v1); atomicAdd(a + 2, v2); atomicAdd(a + 3, v3);
+}
+
+inline int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CPIC_OK : CPIC_ECUDA;
+}
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Common grid validation: periodic, one ghost layer, cell count in int range.
+int check_grid(const cpic_grid* g);
+
+}  // namespace cpic

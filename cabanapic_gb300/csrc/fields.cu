@@ -1,0 +1,452 @@
+// fields.cu -- per-cell kernels of the step: interpolator load, accumulator
+// clear/unload, periodic ghost fold and copy, the EM Yee updates and the
+// field-energy reduction.
+//
+// Reference: src/interpolator.cpp:4-172, src/accumulator.cpp:5-122,
+// src/fields.h:11-271 (ghosts), 556-719 (EM solver), 722-763 (dump_energies).
+//
+// The cell arrays keep the reference's AoSoA layout (32-cell blocks), so one
+// warp handling 32 consecutive x cells reads and writes each member as one
+// 128-byte line.  Arithmetic follows the reference operation by operation and
+// this file is compiled with --fmad=false, so every field value is
+// bit-identical to a CPU build of the reference without FMA contraction.  The
+// energy reduction accumulates in double (the reference sums in real_t) with a
+// fixed reduction tree, so it is deterministic.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace cpic {
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(int64_t n, int threads = kThreads) {
+  int64_t b = (n + threads - 1) / threads;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+// ------------------------------------------------------------ interpolator
+// load_interpolator_array (interpolator.cpp:48-136): interior cells.
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridDev g) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)g.nx * g.ny * g.nz) return;
+  const int x = (int)(t % g.nx) + 1;
+  const int y = (int)((t / g.nx) % g.ny) + 1;
+  const int z = (int)(t / ((int64_t)g.nx * g.ny)) + 1;
+  const int i = g.vox(x, y, z);
+  const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+  const R fourth = 1.0 / 4.0, half = 1.0 / 2.0;
+  auto four = [&](int m0, R w0, R w1, R w2, R w3) {
+    I[cell_at<18>(i, m0 + 0)] = fourth * ((w3 + w0) + (w1 + w2));
+    I[cell_at<18>(i, m0 + 1)] = fourth * ((w3 - w0) + (w1 - w2));
+    I[cell_at<18>(i, m0 + 2)] = fourth * ((w3 - w0) - (w1 - w2));
+    I[cell_at<18>(i, m0 + 3)] = fourth * ((w3 + w0) - (w1 + w2));
+  };
+  four(CPIC_I_EX, F[cell_at<9>(i, CPIC_F_EX)], F[cell_at<9>(i + oy, CPIC_F_EX)],
+       F[cell_at<9>(i + oz, CPIC_F_EX)], F[cell_at<9>(i + oy + oz, CPIC_F_EX)]);
+  four(CPIC_I_EY, F[cell_at<9>(i, CPIC_F_EY)], F[cell_at<9>(i + oz, CPIC_F_EY)],
+       F[cell_at<9>(i + ox, CPIC_F_EY)], F[cell_at<9>(i + ox + oz, CPIC_F_EY)]);
+  four(CPIC_I_EZ, F[cell_at<9>(i, CPIC_F_EZ)], F[cell_at<9>(i + ox, CPIC_F_EZ)],
+       F[cell_at<9>(i + oy, CPIC_F_EZ)], F[cell_at<9>(i + ox + oy, CPIC_F_EZ)]);
+  R w0 = F[cell_at<9>(i, CPIC_F_CBX)], w1 = F[cell_at<9>(i + ox, CPIC_F_CBX)];
+  I[cell_at<18>(i, CPIC_I_CBX)] = half * (w1 + w0);
+  I[cell_at<18>(i, CPIC_I_DCBXDX)] = half * (w1 - w0);
+  w0 = F[cell_at<9>(i, CPIC_F_CBY)]; w1 = F[cell_at<9>(i + oy, CPIC_F_CBY)];
+  I[cell_at<18>(i, CPIC_I_CBY)] = half * (w1 + w0);
+  I[cell_at<18>(i, CPIC_I_DCBYDY)] = half * (w1 - w0);
+  w0 = F[cell_at<9>(i, CPIC_F_CBZ)]; w1 = F[cell_at<9>(i + oz, CPIC_F_CBZ)];
+  I[cell_at<18>(i, CPIC_I_CBZ)] = half * (w1 + w0);
+  I[cell_at<18>(i, CPIC_I_DCBZDZ)] = half * (w1 - w0);
+}
+
+// ------------------------------------------------------------ accumulator
+// unload_accumulator_array (accumulator.cpp:71-110): cells [1, n+1] per axis.
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+unload_kernel(R* __restrict__ F, const R* __restrict__ A, const GridDev g, R cx, R cy, R cz) {
+  const int ex = g.nx + 1, ey = g.ny + 1, ez = g.nz + 1;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)ex * ey * ez) return;
+  const int x = (int)(t % ex) + 1;
+  const int y = (int)((t / ex) % ey) + 1;
+  const int z = (int)(t / ((int64_t)ex * ey)) + 1;
+  const int i = g.vox(x, y, z);
+  const int xd = g.vox(x - 1, y, z), yd = g.vox(x, y - 1, z), zd = g.vox(x, y, z - 1);
+  const int xzd = g.vox(x - 1, y, z - 1), xyd = g.vox(x - 1, y - 1, z), yzd = g.vox(x, y - 1, z - 1);
+  auto a = [&](int c, int k) { return __ldg(A + (size_t)c * 12 + k); };
+  F[cell_at<9>(i, CPIC_F_JFX)] = cx * (a(i, 0) + a(yd, 1) + a(zd, 2) + a(yzd, 3));
+  F[cell_at<9>(i, CPIC_F_JFY)] = cy * (a(i, 4) + a(zd, 5) + a(xd, 6) + a(xzd, 7));
+  F[cell_at<9>(i, CPIC_F_JFZ)] = cz * (a(i, 8) + a(xd, 9) + a(yd, 10) + a(xyd, 11));
+}
+
+// ------------------------------------------------------------ ghosts
+// Periodic fold (+=) of the jf ghosts, serial_update_ghosts (fields.h:102-271).
+// One block per outer index and component; the two passes of a component run
+// in the reference's order, separated by a block barrier.
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+current_fold_kernel(R* __restrict__ F, const GridDev g) {
+  const int comp = blockIdx.y;
+  const int o = blockIdx.x + 1;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  if (comp == 0 && o <= nx) {  // jfx, x = o: fold y then z
+    for (int z = 1 + threadIdx.x; z <= nz + 1; z += blockDim.x)
+      F[cell_at<9>(g.vox(o, 1, z), CPIC_F_JFX)] += F[cell_at<9>(g.vox(o, ny + 1, z), CPIC_F_JFX)];
+    __syncthreads();
+    for (int y = 1 + threadIdx.x; y <= ny + 1; y += blockDim.x)
+      F[cell_at<9>(g.vox(o, y, 1), CPIC_F_JFX)] += F[cell_at<9>(g.vox(o, y, nz + 1), CPIC_F_JFX)];
+  } else if (comp == 1 && o <= ny) {  // jfy, y = o: fold z then x
+    for (int x = 1 + threadIdx.x; x <= nx + 1; x += blockDim.x)
+      F[cell_at<9>(g.vox(x, o, 1), CPIC_F_JFY)] += F[cell_at<9>(g.vox(x, o, nz + 1), CPIC_F_JFY)];
+    __syncthreads();
+    for (int z = 1 + threadIdx.x; z <= nz + 1; z += blockDim.x)
+      F[cell_at<9>(g.vox(1, o, z), CPIC_F_JFY)] += F[cell_at<9>(g.vox(nx + 1, o, z), CPIC_F_JFY)];
+  } else if (comp == 2 && o <= nz) {  // jfz, z = o: fold x then y
+    for (int y = 1 + threadIdx.x; y <= ny + 1; y += blockDim.x)
+      F[cell_at<9>(g.vox(1, y, o), CPIC_F_JFZ)] += F[cell_at<9>(g.vox(nx + 1, y, o), CPIC_F_JFZ)];
+    __syncthreads();
+    for (int x = 1 + threadIdx.x; x <= nx + 1; x += blockDim.x)
+      F[cell_at<9>(g.vox(x, 1, o), CPIC_F_JFZ)] += F[cell_at<9>(g.vox(x, ny + 1, o), CPIC_F_JFZ)];
+  }
+}
+
+// Periodic ghost copy of three members, serial_update_ghosts_B
+// (fields.h:11-100).  The reference's three face passes copy interior values
+// only, so each ghost cell ends up holding the interior cell at its periodic
+// image; one pass over the ghost shell does the same copies.
+__device__ __forceinline__ int wrap(int c, int n) { return c == 0 ? n : (c == n + 1 ? 1 : c); }
+
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+ghost_copy_kernel(R* __restrict__ F, const GridDev g, int m0) {
+  const int sx = g.sx, sy = g.sy, nx = g.nx, ny = g.ny, nz = g.nz;
+  const int64_t zfaces = 2LL * sx * sy;        // z = 0 and z = nz+1, all x, y
+  const int64_t yfaces = 2LL * sx * nz;        // y = 0 and y = ny+1, all x, z in [1, nz]
+  const int64_t xfaces = 2LL * ny * nz;        // x = 0 and x = nx+1, y in [1, ny], z in [1, nz]
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int x, y, z;
+  if (t < zfaces) {
+    const int64_t plane = t / ((int64_t)sx * sy), r = t % ((int64_t)sx * sy);
+    z = plane ? nz + 1 : 0; y = (int)(r / sx); x = (int)(r % sx);
+  } else if ((t -= zfaces) < yfaces) {
+    const int64_t plane = t / ((int64_t)sx * nz), r = t % ((int64_t)sx * nz);
+    y = plane ? ny + 1 : 0; z = (int)(r / sx) + 1; x = (int)(r % sx);
+  } else if ((t -= yfaces) < xfaces) {
+    const int64_t plane = t / ((int64_t)ny * nz), r = t % ((int64_t)ny * nz);
+    x = plane ? nx + 1 : 0; z = (int)(r / ny) + 1; y = (int)(r % ny) + 1;
+  } else {
+    return;
+  }
+  const int to = g.vox(x, y, z);
+  const int from = g.vox(wrap(x, nx), wrap(y, ny), wrap(z, nz));
+  F[cell_at<9>(to, m0 + 0)] = F[cell_at<9>(from, m0 + 0)];
+  F[cell_at<9>(to, m0 + 1)] = F[cell_at<9>(from, m0 + 1)];
+  F[cell_at<9>(to, m0 + 2)] = F[cell_at<9>(from, m0 + 2)];
+}
+
+template <class R>
+static int ghost_copy(R* F, const GridDev& g, int m0, cudaStream_t s) {
+  const int64_t n = 2LL * g.sx * g.sy + 2LL * g.sx * g.nz + 2LL * g.ny * g.nz;
+  ghost_copy_kernel<R><<<blocks_for(n), kThreads, 0, s>>>(F, g, m0);
+  return launch_status();
+}
+
+// ------------------------------------------------------------ EM solver
+// EM_Field_Solver::advance_b (fields.h:692-717): interior cells.
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+advance_b_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)g.nx * g.ny * g.nz) return;
+  const int x = (int)(t % g.nx) + 1;
+  const int y = (int)((t / g.nx) % g.ny) + 1;
+  const int z = (int)(t / ((int64_t)g.nx * g.ny)) + 1;
+  const int f0 = g.vox(x, y, z), fx = f0 + 1, fy = f0 + g.sx, fz = f0 + g.sx * g.sy;
+  auto e = [&](int c, int m) { return F[cell_at<9>(c, m)]; };
+  const R ex0 = e(f0, CPIC_F_EX), ey0 = e(f0, CPIC_F_EY), ez0 = e(f0, CPIC_F_EZ);
+  F[cell_at<9>(f0, CPIC_F_CBX)] -= (py * (e(fy, CPIC_F_EZ) - ez0) - pz * (e(fz, CPIC_F_EY) - ey0));
+  F[cell_at<9>(f0, CPIC_F_CBY)] -= (pz * (e(fz, CPIC_F_EX) - ex0) - px * (e(fx, CPIC_F_EZ) - ez0));
+  F[cell_at<9>(f0, CPIC_F_CBZ)] -= (px * (e(fx, CPIC_F_EY) - ey0) - py * (e(fy, CPIC_F_EX) - ex0));
+}
+
+// EM_Field_Solver::advance_e (fields.h:646-664): cells [1, n+1] per axis.
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+advance_e_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz, R cj) {
+  const int ex = g.nx + 1, ey = g.ny + 1, ez = g.nz + 1;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)ex * ey * ez) return;
+  const int x = (int)(t % ex) + 1;
+  const int y = (int)((t / ex) % ey) + 1;
+  const int z = (int)(t / ((int64_t)ex * ey)) + 1;
+  const int f0 = g.vox(x, y, z), fx = f0 - 1, fy = f0 - g.sx, fz = f0 - g.sx * g.sy;
+  auto b = [&](int c, int m) { return F[cell_at<9>(c, m)]; };
+  const R bx0 = b(f0, CPIC_F_CBX), by0 = b(f0, CPIC_F_CBY), bz0 = b(f0, CPIC_F_CBZ);
+  R* pex = F + cell_at<9>(f0, CPIC_F_EX);
+  R* pey = F + cell_at<9>(f0, CPIC_F_EY);
+  R* pez = F + cell_at<9>(f0, CPIC_F_EZ);
+  *pex = *pex + (-cj * b(f0, CPIC_F_JFX)) + (py * (bz0 - b(fy, CPIC_F_CBZ)) - pz * (by0 - b(fz, CPIC_F_CBY)));
+  *pey = *pey + (-cj * b(f0, CPIC_F_JFY)) + (pz * (bx0 - b(fz, CPIC_F_CBX)) - px * (bz0 - b(fx, CPIC_F_CBZ)));
+  *pez = *pez + (-cj * b(f0, CPIC_F_JFZ)) + (px * (by0 - b(fx, CPIC_F_CBY)) - py * (bx0 - b(fy, CPIC_F_CBX)));
+}
+
+// ------------------------------------------------------------ energies
+// e_energy / b_energy (fields.h:556-615) accumulated in double.  A fixed grid
+// of kEnergyBlocks blocks writes per-block partial sums to scratch; the last
+// block to finish (counter in scratch) adds them in block order.
+constexpr int kEnergyBlocks = 592;  // fixed, so the sum order is device-independent
+
+struct EnergyScratch {
+  double part[2 * kEnergyBlocks];
+  unsigned int done;
+};
+
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+energy_kernel(const R* __restrict__ F, const GridDev g, double* __restrict__ out,
+              EnergyScratch* __restrict__ sc) {
+  __shared__ double se[kThreads / 32], sb[kThreads / 32];
+  __shared__ bool last;
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  double e = 0.0, bb = 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % g.nx) + 1;
+    const int y = (int)((t / g.nx) % g.ny) + 1;
+    const int z = (int)(t / ((int64_t)g.nx * g.ny)) + 1;
+    const int i = g.vox(x, y, z);
+    const double a0 = F[cell_at<9>(i, CPIC_F_EX)], a1 = F[cell_at<9>(i, CPIC_F_EY)], a2 = F[cell_at<9>(i, CPIC_F_EZ)];
+    const double c0 = F[cell_at<9>(i, CPIC_F_CBX)], c1 = F[cell_at<9>(i, CPIC_F_CBY)], c2 = F[cell_at<9>(i, CPIC_F_CBZ)];
+    e += a0 * a0 + a1 * a1 + a2 * a2;
+    bb += c0 * c0 + c1 * c1 + c2 * c2;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_xor_sync(kFull, e, o);
+    bb += __shfl_xor_sync(kFull, bb, o);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { se[w] = e; sb[w] = bb; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double te = 0.0, tb = 0.0;
+    for (int k = 0; k < kThreads / 32; ++k) { te += se[k]; tb += sb[k]; }
+    sc->part[2 * blockIdx.x] = te;
+    sc->part[2 * blockIdx.x + 1] = tb;
+    __threadfence();
+    const unsigned prev = atomicAdd(&sc->done, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double te = 0.0, tb = 0.0;
+    for (unsigned k = 0; k < gridDim.x; ++k) {
+      te += __ldcg(&sc->part[2 * k]);
+      tb += __ldcg(&sc->part[2 * k + 1]);
+    }
+    out[0] = te * 0.5;
+    out[1] = tb * 0.5;
+    sc->done = 0;  // ready for the next call
+  }
+}
+
+// ------------------------------------------------------------ host side
+template <class R>
+static int typed_load_interp(const void* f, void* i, const GridDev& g, cudaStream_t s) {
+  load_interpolator_kernel<R><<<blocks_for((int64_t)g.nx * g.ny * g.nz), kThreads, 0, s>>>(
+      static_cast<const R*>(f), static_cast<R*>(i), g);
+  return launch_status();
+}
+
+template <class R>
+static int typed_unload(void* f, const void* a, const GridDev& g, double dx, double dy, double dz,
+                        double dt, cudaStream_t s) {
+  const R rdx = (R)dx, rdy = (R)dy, rdz = (R)dz, rdt = (R)dt;
+  // cx = 0.25 / (dy*dz*dt) with the double literal (accumulator.cpp:66-68)
+  const R cx = (R)(0.25 / (double)(R)(rdy * rdz * rdt));
+  const R cy = (R)(0.25 / (double)(R)(rdz * rdx * rdt));
+  const R cz = (R)(0.25 / (double)(R)(rdx * rdy * rdt));
+  const int64_t n = (int64_t)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
+  unload_kernel<R><<<blocks_for(n), kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const R*>(a), g,
+                                                      cx, cy, cz);
+  return launch_status();
+}
+
+template <class R>
+static int typed_advance_b(void* f, double px, double py, double pz, const GridDev& g, cudaStream_t s) {
+  advance_b_kernel<R><<<blocks_for((int64_t)g.nx * g.ny * g.nz), kThreads, 0, s>>>(
+      static_cast<R*>(f), g, (R)px, (R)py, (R)pz);
+  int rc = launch_status();
+  if (rc) return rc;
+  return ghost_copy<R>(static_cast<R*>(f), g, CPIC_F_CBX, s);
+}
+
+template <class R>
+static int typed_advance_e(void* f, double px, double py, double pz, double dt_eps0,
+                           const GridDev& g, cudaStream_t s) {
+  R* F = static_cast<R*>(f);
+  int outer = g.nx > g.ny ? g.nx : g.ny;
+  outer = outer > g.nz ? outer : g.nz;
+  current_fold_kernel<R><<<dim3((unsigned)outer, 3), 128, 0, s>>>(F, g);
+  int rc = launch_status();
+  if (rc) return rc;
+  rc = ghost_copy<R>(F, g, CPIC_F_JFX, s);
+  if (rc) return rc;
+  const int64_t n = (int64_t)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
+  advance_e_kernel<R><<<blocks_for(n), kThreads, 0, s>>>(F, g, (R)px, (R)py, (R)pz, (R)dt_eps0);
+  return launch_status();
+}
+
+template <class R>
+static int typed_energies(const void* f, const GridDev& g, double* out, void* scratch, cudaStream_t s) {
+  energy_kernel<R><<<kEnergyBlocks, kThreads, 0, s>>>(static_cast<const R*>(f), g, out,
+                                                      static_cast<EnergyScratch*>(scratch));
+  return launch_status();
+}
+
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  if (cached[dev] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 1;
+  }
+  return cached[dev];
+}
+
+int check_grid(const cpic_grid* g) {
+  if (!g) return CPIC_EINVAL;
+  if (g->nx < 1 || g->ny < 1 || g->nz < 1) return CPIC_EINVAL;
+  if (g->boundary != CPIC_PERIODIC && g->boundary != CPIC_REFLECT) return CPIC_EINVAL;
+  if (g->boundary == CPIC_REFLECT) return CPIC_EUNSUPPORTED;  // the reference exit(1)s
+  if (g->num_ghosts != 1) return CPIC_EUNSUPPORTED;           // the reference assumes one layer
+  const int64_t cells = (g->nx + 2) * (g->ny + 2) * (g->nz + 2);
+  if (g->nx > (1 << 20) || g->ny > (1 << 20) || g->nz > (1 << 20) || cells > 0x7fffffffLL - 64)
+    return CPIC_EINVAL;
+  return CPIC_OK;
+}
+
+}  // namespace cpic
+
+using namespace cpic;
+
+#define CPIC_CHECK_PREC(p) \
+  if ((p) != CPIC_FLOAT && (p) != CPIC_DOUBLE) return CPIC_EINVAL
+
+extern "C" int cpic_load_interpolator(const void* fields, void* interpolators, const cpic_grid* grid,
+                                      int32_t precision, cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields || !interpolators) return CPIC_EINVAL;
+  const GridDev g = make_grid(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return precision == CPIC_FLOAT ? typed_load_interp<float>(fields, interpolators, g, s)
+                                 : typed_load_interp<double>(fields, interpolators, g, s);
+}
+
+extern "C" int cpic_initialize_interpolator(void* interpolators, int64_t num_cells, int32_t precision,
+                                            cpic_stream_t stream) {
+  CPIC_CHECK_PREC(precision);
+  if (!interpolators || num_cells < 0) return CPIC_EINVAL;
+  const size_t bytes = cpic_cell_array_bytes(num_cells, CPIC_INTERP_MEMBERS, precision);
+  return cudaMemsetAsync(interpolators, 0, bytes, reinterpret_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? CPIC_OK : CPIC_ECUDA;
+}
+
+extern "C" int cpic_clear_accumulator(void* accumulators, int64_t num_cells, int32_t precision,
+                                      cpic_stream_t stream) {
+  CPIC_CHECK_PREC(precision);
+  if (!accumulators || num_cells < 0) return CPIC_EINVAL;
+  const size_t bytes = (size_t)num_cells * CPIC_ACC_VALUES * (size_t)precision;
+  return cudaMemsetAsync(accumulators, 0, bytes, reinterpret_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? CPIC_OK : CPIC_ECUDA;
+}
+
+extern "C" int cpic_unload_accumulator(void* fields, const void* accumulators, const cpic_grid* grid,
+                                       double dx, double dy, double dz, double dt, int32_t precision,
+                                       cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields || !accumulators) return CPIC_EINVAL;
+  const GridDev g = make_grid(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return precision == CPIC_FLOAT ? typed_unload<float>(fields, accumulators, g, dx, dy, dz, dt, s)
+                                 : typed_unload<double>(fields, accumulators, g, dx, dy, dz, dt, s);
+}
+
+extern "C" int cpic_advance_b(void* fields, double px, double py, double pz, const cpic_grid* grid,
+                              int32_t precision, cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields) return CPIC_EINVAL;
+  const GridDev g = make_grid(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return precision == CPIC_FLOAT ? typed_advance_b<float>(fields, px, py, pz, g, s)
+                                 : typed_advance_b<double>(fields, px, py, pz, g, s);
+}
+
+extern "C" int cpic_advance_e(void* fields, double px, double py, double pz, const cpic_grid* grid,
+                              double dt_eps0, int32_t precision, cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields) return CPIC_EINVAL;
+  const GridDev g = make_grid(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return precision == CPIC_FLOAT ? typed_advance_e<float>(fields, px, py, pz, dt_eps0, g, s)
+                                 : typed_advance_e<double>(fields, px, py, pz, dt_eps0, g, s);
+}
+
+extern "C" size_t cpic_energy_scratch_bytes(void) { return sizeof(EnergyScratch); }
+
+extern "C" int cpic_field_energies(const void* fields, const cpic_grid* grid, int32_t precision,
+                                   double* d_out, void* d_scratch, size_t scratch_bytes,
+                                   cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields || !d_out || !d_scratch) return CPIC_EINVAL;
+  if (scratch_bytes < sizeof(EnergyScratch)) return CPIC_ESCRATCH;
+  if (((uintptr_t)d_scratch & 7) || ((uintptr_t)d_out & 7)) return CPIC_EINVAL;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  // the completion counter must start at zero: clear it (the kernel leaves it zero)
+  if (cudaMemsetAsync(&static_cast<EnergyScratch*>(d_scratch)->done, 0, sizeof(unsigned), s) != cudaSuccess)
+    return CPIC_ECUDA;
+  const GridDev g = make_grid(grid);
+  return precision == CPIC_FLOAT ? typed_energies<float>(fields, g, d_out, d_scratch, s)
+                                 : typed_energies<double>(fields, g, d_out, d_scratch, s);
+}
+
+extern "C" int cpic_status_clear(int32_t* d_status, cpic_stream_t stream) {
+  if (!d_status) return CPIC_EINVAL;
+  return cudaMemsetAsync(d_status, 0, sizeof(int32_t), reinterpret_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? CPIC_OK : CPIC_ECUDA;
+}
+
+extern "C" int cpic_status_read(const int32_t* d_status, cpic_stream_t stream, int32_t* h_status) {
+  if (!d_status || !h_status) return CPIC_EINVAL;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(h_status, d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return CPIC_ECUDA;
+  return cudaStreamSynchronize(s) == cudaSuccess ? CPIC_OK : CPIC_ECUDA;
+}
+
+extern "C" int cpic_version(void) { return 1; }
+
+extern "C" const char* cpic_strerror(int code) {
+  switch (code) {
+    case CPIC_OK: return "ok";
+    case CPIC_EINVAL: return "invalid argument";
+    case CPIC_EUNSUPPORTED: return "unsupported (Reflect boundary or num_ghosts != 1)";
+    case CPIC_ECUDA: return "CUDA error";
+    case CPIC_ESCRATCH: return "scratch buffer too small";
+    default: return "unknown cpic error";
+  }
+}

@@ -1,0 +1,226 @@
+// sort.cu -- counting sort of the particle AoSoA by cell index.
+//
+// The reference leaves its sort commented out (example/example.cpp:226-228,
+// Cabana::sortByKey on the cell slice).  Sorting every few steps keeps a
+// warp's particles in one or two cells, which turns the push's 18-coefficient
+// gather into a broadcast and lets its deposit reduce within the warp.
+//
+// Passes (keys are cell indices in [0, num_cells); an out-of-range key sorts
+// after all valid ones):
+//   1. rank:    per particle, its arrival rank in its cell (warp-aggregated
+//               atomics: one atomic per distinct cell per warp)
+//   2. scan:    exclusive prefix sum of the per-cell counts -> cell offsets
+//   3. scatter: perm[offset[cell] + rank] = particle index
+//   4. gather:  particles[d] = copy[perm[d]], member by member (coalesced writes)
+// The order within a cell depends on atomic arrival order.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace cpic {
+
+constexpr int kSortThreads = 256;
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct SortPlan {
+  size_t counts_off, sums_off, rank_off, perm_off, copy_off, total;
+  int64_t nkeys, nscan_blocks;
+};
+
+static SortPlan plan_sort(int64_t n, int64_t num_cells, int prec, int vl) {
+  SortPlan p;
+  p.nkeys = num_cells + 1;  // last key collects out-of-range cells
+  p.nscan_blocks = (p.nkeys + kScanTile - 1) / kScanTile;
+  size_t off = 0;
+  p.counts_off = off; off += align256(sizeof(int) * (size_t)p.nkeys);
+  p.sums_off = off;   off += align256(sizeof(int) * (size_t)p.nscan_blocks);
+  p.rank_off = off;   off += align256(sizeof(int) * (size_t)n);
+  p.perm_off = off;   off += align256(sizeof(int) * (size_t)n);
+  p.copy_off = off;   off += align256(cpic_particle_list_bytes(n, prec, vl));
+  p.total = off;
+  return p;
+}
+
+template <class R, int VL>
+__global__ void __launch_bounds__(kSortThreads)
+rank_kernel(const unsigned char* __restrict__ part, int n, int num_cells, int* __restrict__ counts,
+            int* __restrict__ rank) {
+  using L = PLayout<R, VL>;
+  const int lane = lane_id();
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < n;
+  int key = -1 - lane;
+  if (valid) {
+    int c = __ldg(reinterpret_cast<const int*>(part + L::cell_off(p)));
+    key = ((unsigned)c < (unsigned)num_cells) ? c : num_cells;
+  }
+  const unsigned peers = __match_any_sync(kFull, key);
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (valid && lane == leader) base = atomicAdd(counts + key, __popc(peers));
+  base = __shfl_sync(kFull, base, leader);
+  if (valid) rank[p] = base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// Block-local exclusive scan of kScanTile ints; returns the tile total.
+__device__ int block_exclusive_scan(int* __restrict__ data, int64_t n, int64_t tile0,
+                                    int* __restrict__ warp_tot) {
+  int v[kScanItems];
+  int local = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int64_t i = tile0 + (int64_t)threadIdx.x * kScanItems + k;
+    v[k] = i < n ? data[i] : 0;
+    local += v[k];
+  }
+  const int lane = lane_id(), w = threadIdx.x >> 5;
+  int incl = local;
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int t = warp_tot[lane];
+    int s = t;
+    for (int o = 1; o < 32; o <<= 1) {
+      int u = __shfl_up_sync(kFull, s, o);
+      if (lane >= o) s += u;
+    }
+    warp_tot[lane] = s - t;  // exclusive prefix of the warp totals
+    if (lane == 31) warp_tot[32] = s;
+  }
+  __syncthreads();
+  int run = warp_tot[w] + incl - local;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int64_t i = tile0 + (int64_t)threadIdx.x * kScanItems + k;
+    if (i < n) data[i] = run;
+    run += v[k];
+  }
+  const int total = warp_tot[32];
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_tiles_kernel(int* __restrict__ data, int64_t n, int* __restrict__ sums) {
+  __shared__ int warp_tot[33];
+  const int total = block_exclusive_scan(data, n, (int64_t)blockIdx.x * kScanTile, warp_tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// One block scans the tile totals, kScanTile at a time with a running carry.
+__global__ void __launch_bounds__(kScanThreads)
+scan_sums_kernel(int* __restrict__ sums, int64_t nsums) {
+  __shared__ int warp_tot[33];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t t0 = 0; t0 < nsums; t0 += kScanTile) {
+    const int c = carry;
+    __syncthreads();
+    const int total = block_exclusive_scan(sums, nsums, t0, warp_tot);
+    for (int64_t i = t0 + threadIdx.x; i < nsums && i < t0 + kScanTile; i += blockDim.x) sums[i] += c;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c + total;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_add_kernel(int* __restrict__ data, int64_t n, const int* __restrict__ sums) {
+  const int add = sums[blockIdx.x];
+  const int64_t t0 = (int64_t)blockIdx.x * kScanTile;
+  for (int k = threadIdx.x; k < kScanTile; k += blockDim.x) {
+    const int64_t i = t0 + k;
+    if (i < n) data[i] += add;
+  }
+}
+
+template <class R, int VL>
+__global__ void __launch_bounds__(kSortThreads)
+scatter_kernel(const unsigned char* __restrict__ part, int n, int num_cells,
+               const int* __restrict__ offsets, const int* __restrict__ rank, int* __restrict__ perm) {
+  using L = PLayout<R, VL>;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  int c = __ldg(reinterpret_cast<const int*>(part + L::cell_off(p)));
+  c = ((unsigned)c < (unsigned)num_cells) ? c : num_cells;
+  perm[offsets[c] + rank[p]] = (int)p;
+}
+
+template <class R, int VL>
+__global__ void __launch_bounds__(kSortThreads)
+gather_kernel(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, int n,
+              const int* __restrict__ perm) {
+  using L = PLayout<R, VL>;
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= n) return;
+  const int s = perm[d];
+#pragma unroll
+  for (int m = 0; m < 7; ++m)
+    *reinterpret_cast<R*>(dst + L::off(d, m)) = __ldg(reinterpret_cast<const R*>(src + L::off(s, m)));
+  *reinterpret_cast<int*>(dst + L::cell_off(d)) = __ldg(reinterpret_cast<const int*>(src + L::cell_off(s)));
+}
+
+template <class R, int VL>
+static int sort_typed(void* particles, int n, int num_cells, const SortPlan& pl, unsigned char* sc,
+                      cudaStream_t s) {
+  int* counts = reinterpret_cast<int*>(sc + pl.counts_off);
+  int* sums = reinterpret_cast<int*>(sc + pl.sums_off);
+  int* rank = reinterpret_cast<int*>(sc + pl.rank_off);
+  int* perm = reinterpret_cast<int*>(sc + pl.perm_off);
+  unsigned char* copy = sc + pl.copy_off;
+  unsigned char* part = static_cast<unsigned char*>(particles);
+  const unsigned pb = (unsigned)(((int64_t)n + kSortThreads - 1) / kSortThreads);
+  if (cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)pl.nkeys, s) != cudaSuccess) return CPIC_ECUDA;
+  rank_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, n, num_cells, counts, rank);
+  scan_tiles_kernel<<<(unsigned)pl.nscan_blocks, kScanThreads, 0, s>>>(counts, pl.nkeys, sums);
+  scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, pl.nscan_blocks);
+  scan_add_kernel<<<(unsigned)pl.nscan_blocks, kScanThreads, 0, s>>>(counts, pl.nkeys, sums);
+  scatter_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, n, num_cells, counts, rank, perm);
+  const size_t bytes = cpic_particle_list_bytes(n, sizeof(R), VL);
+  if (cudaMemcpyAsync(copy, part, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return CPIC_ECUDA;
+  gather_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(copy, part, n, perm);
+  return launch_status();
+}
+
+}  // namespace cpic
+
+using namespace cpic;
+
+extern "C" size_t cpic_sort_scratch_bytes(int64_t num_particles, int64_t num_cells, int32_t precision,
+                                          int32_t particle_vl) {
+  if (num_particles < 0 || num_cells < 1) return 0;
+  if (precision != CPIC_FLOAT && precision != CPIC_DOUBLE) return 0;
+  if (particle_vl != 16 && particle_vl != 32) return 0;
+  return plan_sort(num_particles, num_cells, precision, particle_vl).total;
+}
+
+extern "C" int cpic_sort_particles(void* particles, int64_t num_particles, int64_t num_cells,
+                                   int32_t precision, int32_t particle_vl, void* d_scratch,
+                                   size_t scratch_bytes, cpic_stream_t stream) {
+  if (precision != CPIC_FLOAT && precision != CPIC_DOUBLE) return CPIC_EINVAL;
+  if (particle_vl != 16 && particle_vl != 32) return CPIC_EINVAL;
+  if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
+  if (num_cells < 1 || num_cells > 0x7fffffffLL - 64) return CPIC_EINVAL;
+  if (num_particles == 0) return CPIC_OK;
+  if (!particles || !d_scratch) return CPIC_EINVAL;
+  if (((uintptr_t)particles & 15) || ((uintptr_t)d_scratch & 255)) return CPIC_EINVAL;
+  const SortPlan pl = plan_sort(num_particles, num_cells, precision, particle_vl);
+  if (scratch_bytes < pl.total) return CPIC_ESCRATCH;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  unsigned char* sc = static_cast<unsigned char*>(d_scratch);
+  const int n = (int)num_particles, nc = (int)num_cells;
+  if (precision == CPIC_FLOAT)
+    return particle_vl == 32 ? sort_typed<float, 32>(particles, n, nc, pl, sc, s)
+                             : sort_typed<float, 16>(particles, n, nc, pl, sc, s);
+  return particle_vl == 32 ? sort_typed<double, 32>(particles, n, nc, pl, sc, s)
+                           : sort_typed<double, 16>(particles, n, nc, pl, sc, s);
+}

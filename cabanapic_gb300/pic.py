@@ -1,0 +1,220 @@
+"""The reference's hot-path interface, over the C ABI.
+
+Same names, argument order and meaning as the reference's free functions and
+field solver (src/push.h, src/interpolator.h, src/accumulator.h,
+src/fields.h), so a time loop reads like example/example.cpp.  Each call is
+asynchronous on the current torch CUDA stream.  Argument errors raise
+CpicError immediately; problems found inside kernels are collected in a device
+status word and raised as CpicDeviceError by check_status().
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+
+import numpy as np
+import torch
+
+from . import capi
+from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleList
+
+
+class Boundary(enum.IntEnum):
+    """Boundary, src/input/deck.h:9-12."""
+    Reflect = 0
+    Periodic = 1
+
+
+def _stream(stream=None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+class _Status:
+    """Per-device status words (one int32 each)."""
+
+    def __init__(self):
+        self.words = {}
+
+    def get(self, device=None) -> torch.Tensor:
+        dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        w = self.words.get(dev.index)
+        if w is None:
+            w = torch.zeros(1, dtype=torch.int32, device=dev)
+            self.words[dev.index] = w
+        return w
+
+
+_STATUS = _Status()
+
+
+def status_word(device=None) -> torch.Tensor:
+    return _STATUS.get(device)
+
+
+def check_status(stream=None, device=None, clear: bool = True) -> int:
+    """Synchronises the stream, raises CpicDeviceError if a kernel flagged a problem."""
+    lib = capi.load()
+    w = _STATUS.get(device)
+    out = C.c_int32(0)
+    lib.call("cpic_status_read", w.data_ptr(), _stream(stream), C.byref(out))
+    bits = out.value
+    if clear:
+        lib.call("cpic_status_clear", w.data_ptr(), _stream(stream))
+    if bits:
+        raise capi.CpicDeviceError(bits)
+    return 0
+
+
+def _grid(nx, ny, nz, ng, boundary=Boundary.Periodic):
+    return capi.make_grid(nx, ny, nz, ng, int(boundary))
+
+
+# ---------------------------------------------------------------- push
+def push(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp,
+         a0: AccumulatorArray, g, nx, ny, nz, num_ghosts, boundary, *, true_sqrt: bool = False,
+         stream=None) -> None:
+    """push() (src/push.h:7-300): Boris push, move and current deposit.
+
+    `g` (grid_t*) is accepted and unused, as in the reference.  Adds into a0."""
+    lib = capi.load()
+    prm = capi.CpicPushParams(float(qdt_2mc), float(cdt_dx), float(cdt_dy), float(cdt_dz),
+                              float(qsp), particles.precision, particles.vl,
+                              capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0, 0)
+    if f0.precision != particles.precision or a0.precision != particles.precision:
+        raise capi.CpicError("cpic_push", capi.CPIC_EINVAL, "mixed real_t precisions")
+    grid = _grid(nx, ny, nz, num_ghosts, boundary)
+    if f0.num_cells < grid_cells(nx, ny, nz, num_ghosts) or a0.num_cells < grid_cells(nx, ny, nz, num_ghosts):
+        raise capi.CpicError("cpic_push", capi.CPIC_EINVAL, "cell arrays smaller than the grid")
+    lib.call("cpic_push", particles.ptr, particles.n, f0.ptr, a0.ptr, C.byref(grid), C.byref(prm),
+             _STATUS.get().data_ptr(), _stream(stream))
+
+
+def grid_cells(nx, ny, nz, ng=1) -> int:
+    return (nx + 2 * ng) * (ny + 2 * ng) * (nz + 2 * ng)
+
+
+# ---------------------------------------------------------------- cells
+def load_interpolator_array(fields: FieldArray, interpolators: InterpolatorArray, nx, ny, nz, ng,
+                            *, boundary=Boundary.Periodic, stream=None) -> None:
+    """load_interpolator_array (src/interpolator.cpp:4-124)."""
+    capi.load().call("cpic_load_interpolator", fields.ptr, interpolators.ptr,
+                     C.byref(_grid(nx, ny, nz, ng, boundary)), fields.precision, _stream(stream))
+
+
+def initialize_interpolator(f0: InterpolatorArray, *, stream=None) -> None:
+    """initialize_interpolator (src/interpolator.cpp:125-172): zero fill."""
+    capi.load().call("cpic_initialize_interpolator", f0.ptr, f0.num_cells, f0.precision, _stream(stream))
+
+
+def clear_accumulator_array(fields: FieldArray, accumulators: AccumulatorArray, nx, ny, nz,
+                            *, stream=None) -> None:
+    """clear_accumulator_array (src/accumulator.cpp:5-43)."""
+    capi.load().call("cpic_clear_accumulator", accumulators.ptr, accumulators.num_cells,
+                     accumulators.precision, _stream(stream))
+
+
+def unload_accumulator_array(fields: FieldArray, accumulators: AccumulatorArray, nx, ny, nz, ng,
+                             dx, dy, dz, dt, *, boundary=Boundary.Periodic, stream=None) -> None:
+    """unload_accumulator_array (src/accumulator.cpp:45-122)."""
+    capi.load().call("cpic_unload_accumulator", fields.ptr, accumulators.ptr,
+                     C.byref(_grid(nx, ny, nz, ng, boundary)), float(dx), float(dy), float(dz),
+                     float(dt), fields.precision, _stream(stream))
+
+
+# ---------------------------------------------------------------- fields
+class EMFieldSolver:
+    """Field_Solver<EM_Field_Solver> (src/fields.h:274-379, 550-720).
+
+    The constructor zeroes the fields like Field_Solver's (fields.h:279-315).
+    `boundary` is the deck's BOUNDARY_TYPE, a global in the reference."""
+
+    def __init__(self, fields: FieldArray = None, boundary=Boundary.Periodic):
+        self.boundary = Boundary(boundary)
+        self._out = None
+        self._scratch = None
+        if fields is not None:
+            self.init(fields)
+
+    def init(self, fields: FieldArray) -> None:
+        fields.buf.zero_()
+
+    def advance_b(self, fields: FieldArray, px, py, pz, nx, ny, nz, ng, *, stream=None) -> None:
+        capi.load().call("cpic_advance_b", fields.ptr, float(px), float(py), float(pz),
+                         C.byref(_grid(nx, ny, nz, ng, self.boundary)), fields.precision, _stream(stream))
+
+    def advance_e(self, fields: FieldArray, px, py, pz, nx, ny, nz, ng, dt_eps0, *, stream=None) -> None:
+        capi.load().call("cpic_advance_e", fields.ptr, float(px), float(py), float(pz),
+                         C.byref(_grid(nx, ny, nz, ng, self.boundary)), float(dt_eps0),
+                         fields.precision, _stream(stream))
+
+    def energies_async(self, fields: FieldArray, nx, ny, nz, ng, out: torch.Tensor = None,
+                       *, stream=None) -> torch.Tensor:
+        """Writes [E, B] energies (double) to a device tensor without synchronising."""
+        lib = capi.load()
+        if self._scratch is None:
+            self._scratch = torch.zeros(lib.raw("cpic_energy_scratch_bytes")(), dtype=torch.uint8,
+                                        device=fields.buf.device)
+        if out is None:
+            if self._out is None:
+                self._out = torch.zeros(2, dtype=torch.float64, device=fields.buf.device)
+            out = self._out
+        lib.call("cpic_field_energies", fields.ptr, C.byref(_grid(nx, ny, nz, ng, self.boundary)),
+                 fields.precision, out.data_ptr(), self._scratch.data_ptr(), self._scratch.numel(),
+                 _stream(stream))
+        return out
+
+    def e_energy(self, fields: FieldArray, px, py, pz, nx, ny, nz, ng, *, stream=None) -> float:
+        """EM_Field_Solver::e_energy (fields.h:556-586), accumulated in double."""
+        return float(self.energies_async(fields, nx, ny, nz, ng, stream=stream)[0].item())
+
+    def b_energy(self, fields: FieldArray, px, py, pz, nx, ny, nz, ng, *, stream=None) -> float:
+        """EM_Field_Solver::b_energy (fields.h:588-615), accumulated in double."""
+        return float(self.energies_async(fields, nx, ny, nz, ng, stream=stream)[1].item())
+
+
+def dump_energies(field_solver: EMFieldSolver, fields: FieldArray, step, time, px, py, pz, nx, ny,
+                  nz, ng, path: str = "energies.txt") -> tuple:
+    """dump_energies (src/fields.h:722-763): appends `step time E B` (truncates at step 0)."""
+    e, b = field_solver.energies_async(fields, nx, ny, nz, ng).cpu().tolist()
+    mode = "w" if step == 0 else "a"
+    with open(path, mode) as fh:
+        fh.write(_energy_line(step, time, e, b) + "\n")
+    return e, b
+
+
+def _g6(v: float) -> str:
+    s = f"{v:.6g}"
+    if "e" in s:
+        mant, exp = s.split("e")
+        digits = exp[1:].lstrip("0") or "0"
+        s = f"{mant}e{exp[0]}{digits.zfill(2)}"
+    return s
+
+
+def _energy_line(step, time, e, b) -> str:
+    return f"{step} {_g6(time)} {_g6(e)} {_g6(b)}"
+
+
+# ---------------------------------------------------------------- sort
+class Sorter:
+    """Counting sort of a particle list by cell (scratch owned by this object)."""
+
+    def __init__(self, particles: ParticleList, num_cells: int):
+        lib = capi.load()
+        self.num_cells = int(num_cells)
+        nbytes = lib.raw("cpic_sort_scratch_bytes")(particles.n, self.num_cells, particles.precision,
+                                                   particles.vl)
+        if nbytes == 0:
+            raise capi.CpicError("cpic_sort_scratch_bytes", capi.CPIC_EINVAL, "bad arguments")
+        self.scratch = torch.empty(nbytes, dtype=torch.uint8, device=particles.buf.device)
+
+    def __call__(self, particles: ParticleList, *, stream=None) -> None:
+        capi.load().call("cpic_sort_particles", particles.ptr, particles.n, self.num_cells,
+                         particles.precision, particles.vl, self.scratch.data_ptr(),
+                         self.scratch.numel(), _stream(stream))
+
+
+def sort_particles(particles: ParticleList, num_cells: int, *, stream=None) -> None:
+    Sorter(particles, num_cells)(particles, stream=stream)

@@ -1,0 +1,91 @@
+"""Time-loop driver: the per-step sequence of the reference's main()
+(example/example.cpp:216-271) on one GPU, through the C ABI.
+
+Each step: [cell sort every `sort_interval` steps] -> load_interpolator_array
+-> clear_accumulator_array -> push -> unload_accumulator_array -> advance_b(1/2)
+-> advance_e -> advance_b(1/2) -> field energies (double, kept on the device).
+The per-step particle and field text dumps of the reference are not part of
+the loop (example.cpp:274-277); energies are copied to the host on request.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import decks as D
+from . import pic
+from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleList
+
+
+class Simulation:
+    def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
+                 max_steps: int = None, time_push: bool = False):
+        self.deck = deck
+        self.p = deck.derived()
+        dev = torch.device(device if device is not None else "cuda")
+        self.device = dev
+        R = deck.R
+        nc = deck.num_cells
+        self.particles = ParticleList(deck.num_particles, R, deck.vl, dev)
+        self.interpolators = InterpolatorArray(nc, R, dev)
+        self.accumulators = AccumulatorArray(nc, R, dev)
+        self.fields = FieldArray(nc, R, dev)
+        self.solver = pic.EMFieldSolver(self.fields, deck.boundary)
+        pic.initialize_interpolator(self.interpolators)
+        if particles is None:
+            particles = D.initial_particles(deck)
+        self.particles.upload(particles)
+        self.sort_interval = int(sort_interval)
+        self.sorter = pic.Sorter(self.particles, nc) if self.sort_interval > 0 else None
+        cap = max_steps if max_steps is not None else max(deck.num_steps, 1)
+        self.energy = torch.zeros((cap, 2), dtype=torch.float64, device=dev)
+        self.step_no = 0
+        self.time_push = time_push
+        self.push_events = []
+
+    # ------------------------------------------------------------------
+    def step(self) -> None:
+        d, p = self.deck, self.p
+        nx, ny, nz, ng = d.nx, d.ny, d.nz, d.num_ghosts
+        pic.load_interpolator_array(self.fields, self.interpolators, nx, ny, nz, ng, boundary=d.boundary)
+        pic.clear_accumulator_array(self.fields, self.accumulators, nx, ny, nz)
+        if self.sorter is not None and self.step_no % self.sort_interval == 0:
+            self.sorter(self.particles)
+        if self.time_push:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+        pic.push(self.particles, self.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
+                 p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary)
+        if self.time_push:
+            e1.record()
+            self.push_events.append((e0, e1))
+        pic.unload_accumulator_array(self.fields, self.accumulators, nx, ny, nz, ng,
+                                     p["dx"], p["dy"], p["dz"], p["dt"], boundary=d.boundary)
+        half = d.R(0.5)
+        hpx, hpy, hpz = d.R(half * p["px"]), d.R(half * p["py"]), d.R(half * p["pz"])
+        self.solver.advance_b(self.fields, hpx, hpy, hpz, nx, ny, nz, ng)
+        self.solver.advance_e(self.fields, p["px"], p["py"], p["pz"], nx, ny, nz, ng, p["dt_eps0"])
+        self.solver.advance_b(self.fields, hpx, hpy, hpz, nx, ny, nz, ng)
+        if self.step_no < self.energy.shape[0]:
+            self.solver.energies_async(self.fields, nx, ny, nz, ng, out=self.energy[self.step_no])
+        self.step_no += 1
+
+    def run(self, steps: int) -> None:
+        for _ in range(steps):
+            self.step()
+
+    # ------------------------------------------------------------------
+    def energies(self) -> np.ndarray:
+        """[steps, 2] history of (E, B) field energies, accumulated in double."""
+        return self.energy[: min(self.step_no, self.energy.shape[0])].cpu().numpy()
+
+    def push_times_ms(self) -> list:
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in self.push_events]
+
+    def check_status(self) -> None:
+        pic.check_status()
+
+    def download_particles(self) -> dict:
+        return self.particles.download()

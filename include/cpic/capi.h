@@ -1,0 +1,167 @@
+/* capi.h -- C ABI of the GB300 implementation of CabanaPIC's per-step hot path.
+ *
+ * Every entry point takes raw device pointers into the reference's own array
+ * layouts (see layout.h), plain sizes and a CUDA stream.  Calls are
+ * stream-ordered and asynchronous: none synchronises the host except
+ * cpic_status_read().  The library allocates no device memory: where a kernel
+ * needs scratch space, the caller passes it (see the *_scratch_bytes queries).
+ *
+ * Return codes: CPIC_OK (0); a negative CPIC_E* for a rejected argument or a
+ * CUDA launch error.  Problems found on the device (a particle in a cell
+ * outside the grid, a mover streak cap, a non-finite displacement) are OR-ed
+ * into a caller-owned device status word, read back with cpic_status_read().
+ *
+ * Unlike the reference, which is a header-only template library with no error
+ * reporting (push() is void, move_p's return is ignored, Reflect boundaries
+ * call exit(1)), every entry point validates its arguments and returns a code.
+ */
+#ifndef CPIC_CAPI_H
+#define CPIC_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "layout.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without including the CUDA runtime headers */
+typedef struct CUstream_st* cpic_stream_t;
+
+/* ---------------------------------------------------------------- codes */
+#define CPIC_OK 0
+#define CPIC_EINVAL (-1)       /* null pointer, bad size or bad enum value */
+#define CPIC_EUNSUPPORTED (-2) /* valid in the reference's types but not implemented
+                                  there either (Reflect boundary, num_ghosts != 1) */
+#define CPIC_ECUDA (-3)        /* a CUDA launch or copy returned an error */
+#define CPIC_ESCRATCH (-4)     /* caller-provided scratch too small */
+
+/* device status bits (cpic_status_read) */
+#define CPIC_STATUS_CELL_RANGE 1  /* particle cell index outside [0, num_cells): skipped */
+#define CPIC_STATUS_MOVER_CAP 2   /* move_p streak loop hit its iteration cap */
+#define CPIC_STATUS_NONFINITE 4   /* non-finite displacement met in move_p */
+
+/* Boundary, src/input/deck.h:9-12 */
+#define CPIC_REFLECT 0
+#define CPIC_PERIODIC 1
+
+/* real_t selection: the byte size of real_t (src/types.h:4-8) */
+#define CPIC_FLOAT 4
+#define CPIC_DOUBLE 8
+
+/* cpic_push_params.flags */
+#define CPIC_PUSH_TRUE_SQRT 1  /* real_t=double only: use sqrt() for gamma where the
+                                  reference calls sqrtf() (src/push.h:148,169) */
+
+/* Grid of the run: interior cells nx*ny*nz plus num_ghosts ghost layers;
+ * boundary is the deck's BOUNDARY_TYPE, which the reference's field code reads
+ * from the global deck (src/fields.h:20,112). */
+typedef struct cpic_grid {
+  int64_t nx, ny, nz, num_ghosts;
+  int32_t boundary;
+  int32_t reserved;
+} cpic_grid;
+
+/* Scalar arguments of push() (src/push.h:7-23), in double; they are rounded to
+ * real_t on entry, which is exact for values that were computed in real_t. */
+typedef struct cpic_push_params {
+  double qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp;
+  int32_t precision;   /* CPIC_FLOAT or CPIC_DOUBLE */
+  int32_t particle_vl; /* AoSoA vector length of the particle list: 16 or 32 */
+  int32_t flags;       /* CPIC_PUSH_* */
+  int32_t reserved;
+} cpic_push_params;
+
+/* ---------------------------------------------------------------- queries */
+int cpic_version(void);
+const char* cpic_strerror(int code);
+
+/* ---------------------------------------------------------------- push
+ * Replaces: template<class _accumulator> void push(particle_list_t& particles,
+ *   interpolator_array_t& f0, real_t qdt_2mc, real_t cdt_dx, real_t cdt_dy,
+ *   real_t cdt_dz, real_t qsp, _accumulator& a0, grid_t* g, size_t nx, ny, nz,
+ *   num_ghosts, Boundary boundary)            -- src/push.h:7-300
+ * together with the move_p it calls for cell-crossing particles
+ *                                              -- src/move_p.h:9-374.
+ * Gathers each particle's 18 interpolator coefficients, applies the Boris
+ * push, moves the particle and scatter-adds its 12 current contributions (per
+ * streak for crossers) into `accumulators`, in place.  Like the reference's
+ * ScatterView, it ADDS to the accumulator: clear it first.  `d_status` is a
+ * device int32 the caller owns; problems found are OR-ed into it. */
+int cpic_push(void* particles, int64_t num_particles, const void* interpolators,
+              void* accumulators, const cpic_grid* grid, const cpic_push_params* prm,
+              int32_t* d_status, cpic_stream_t stream);
+
+/* ---------------------------------------------------------------- cells
+ * Replaces: void load_interpolator_array(field_array_t fields,
+ *   interpolator_array_t interpolators, size_t nx, ny, nz, ng)
+ *                                              -- src/interpolator.h:14-21, interpolator.cpp:4-124 */
+int cpic_load_interpolator(const void* fields, void* interpolators, const cpic_grid* grid,
+                           int32_t precision, cpic_stream_t stream);
+
+/* Replaces: void initialize_interpolator(interpolator_array_t& f0)
+ *                                              -- src/interpolator.h:23, interpolator.cpp:125-172 */
+int cpic_initialize_interpolator(void* interpolators, int64_t num_cells, int32_t precision,
+                                 cpic_stream_t stream);
+
+/* Replaces: void clear_accumulator_array(field_array_t& fields,
+ *   accumulator_array_t& accumulators, size_t nx, ny, nz)
+ *                                              -- src/accumulator.h:15-21, accumulator.cpp:5-43 */
+int cpic_clear_accumulator(void* accumulators, int64_t num_cells, int32_t precision,
+                           cpic_stream_t stream);
+
+/* Replaces: void unload_accumulator_array(field_array_t& fields,
+ *   accumulator_array_t& accumulators, size_t nx, ny, nz, ng, real_t dx, dy, dz, dt)
+ *                                              -- src/accumulator.h:23-32, accumulator.cpp:45-122 */
+int cpic_unload_accumulator(void* fields, const void* accumulators, const cpic_grid* grid,
+                            double dx, double dy, double dz, double dt, int32_t precision,
+                            cpic_stream_t stream);
+
+/* Replaces: Field_Solver<EM_Field_Solver>::advance_b(field_array_t&, real_t px, py, pz,
+ *   size_t nx, ny, nz, ng)                     -- src/fields.h:352-364, 668-719
+ * (cB update over the interior, then the periodic ghost copy of cB). */
+int cpic_advance_b(void* fields, double px, double py, double pz, const cpic_grid* grid,
+                   int32_t precision, cpic_stream_t stream);
+
+/* Replaces: Field_Solver<EM_Field_Solver>::advance_e(field_array_t&, real_t px, py, pz,
+ *   size_t nx, ny, nz, ng, real_t dt_eps0)     -- src/fields.h:365-378, 618-665
+ * (periodic fold of the jf ghosts, ghost copy of jf, then the E update). */
+int cpic_advance_e(void* fields, double px, double py, double pz, const cpic_grid* grid,
+                   double dt_eps0, int32_t precision, cpic_stream_t stream);
+
+/* Replaces: EM_Field_Solver::e_energy and b_energy (src/fields.h:556-615), as
+ * used by dump_energies (src/fields.h:722-763): writes {0.5*sum E^2,
+ * 0.5*sum cB^2} over the interior, accumulated in double, to d_out[0..1]
+ * (device memory).  The sum order is fixed (deterministic).  `d_scratch` must
+ * hold cpic_energy_scratch_bytes() bytes of device memory; its contents on
+ * entry do not matter. */
+size_t cpic_energy_scratch_bytes(void);
+int cpic_field_energies(const void* fields, const cpic_grid* grid, int32_t precision,
+                        double* d_out, void* d_scratch, size_t scratch_bytes,
+                        cpic_stream_t stream);
+
+/* ---------------------------------------------------------------- sort
+ * Counting sort of the particle list by cell index, in place.  The reference
+ * leaves this step commented out (example/example.cpp:226-228, Cabana::sortByKey);
+ * here it keeps the push's gathers and deposits local.  The order of particles
+ * that share a cell is not specified.  `d_scratch` must hold
+ * cpic_sort_scratch_bytes(...) bytes of device memory. */
+size_t cpic_sort_scratch_bytes(int64_t num_particles, int64_t num_cells, int32_t precision,
+                               int32_t particle_vl);
+int cpic_sort_particles(void* particles, int64_t num_particles, int64_t num_cells,
+                        int32_t precision, int32_t particle_vl, void* d_scratch,
+                        size_t scratch_bytes, cpic_stream_t stream);
+
+/* ---------------------------------------------------------------- status */
+/* Clears the device status word (stream-ordered). */
+int cpic_status_clear(int32_t* d_status, cpic_stream_t stream);
+/* Synchronises `stream` and copies the status word to *h_status. */
+int cpic_status_read(const int32_t* d_status, cpic_stream_t stream, int32_t* h_status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPIC_CAPI_H */

@@ -73,6 +73,9 @@ struct Grid {
   long vox(long x, long y, long z) const { return x + sx() * (y + sy() * z); }
 };
 
+// Per-cell loops below run under OpenMP: every iteration writes only its own
+// cell, so the results do not depend on the thread count.
+
 // Accumulator sink: the reference scatter-adds into View<real_t*[3][4]>.  The
 // optional abs/count arrays record, per (cell, comp, quadrant), the sum of
 // |contribution| and the number of terms; the tests use them to bound the
@@ -330,6 +333,7 @@ void load_interpolator(const R* fields, R* interp, const Grid& g) {
     I(i, m0 + 2) = fourth * ((w3 - w0) - (w1 - w2));
     I(i, m0 + 3) = fourth * ((w3 + w0) - (w1 + w2));
   };
+#pragma omp parallel for schedule(static)
   for (long z = g.ng; z < g.nz + g.ng; ++z)
     for (long y = g.ng; y < g.ny + g.ng; ++y)
       for (long x = g.ng; x < g.nx + g.ng; ++x) {
@@ -355,6 +359,7 @@ void unload_accumulator(R* fields, const R* acc, const Grid& g, R dx, R dy, R dz
   R cy = 0.25 / (dz * dx * dt);
   R cz = 0.25 / (dx * dy * dt);
   auto A = [&](long c, int comp, int q) { return acc[(size_t)c * 12 + comp * 4 + q]; };
+#pragma omp parallel for schedule(static)
   for (long z = g.ng; z <= g.nz + g.ng; ++z)
     for (long y = g.ng; y <= g.ny + g.ng; ++y)
       for (long x = g.ng; x <= g.nx + g.ng; ++x) {
@@ -416,6 +421,7 @@ void current_fold(R* fields, const Grid& g) {
 template <class R>
 void advance_b(R* fields, R px, R py, R pz, const Grid& g) {
   CellSoA<R, kFieldMembers> F{fields};
+#pragma omp parallel for schedule(static)
   for (long z = 1; z < g.nz + 1; ++z)
     for (long y = 1; y < g.ny + 1; ++y)
       for (long x = 1; x < g.nx + 1; ++x) {
@@ -434,6 +440,7 @@ void advance_e(R* fields, R px, R py, R pz, const Grid& g, R dt_eps0) {
   current_fold<R>(fields, g);
   ghost_copy<R>(fields, g, F_JFX);
   const R cj = dt_eps0;
+#pragma omp parallel for schedule(static)
   for (long z = 1; z < g.nz + 2; ++z)
     for (long y = 1; y < g.ny + 2; ++y)
       for (long x = 1; x < g.nx + 2; ++x) {

@@ -1,0 +1,63 @@
+"""Seeded random states for the parity tests (test infrastructure)."""
+from __future__ import annotations
+
+import numpy as np
+
+import oracle
+from cabanapic_gb300 import layout as L
+
+
+def random_state(nx=6, ny=5, nz=4, n=4000, seed=0, real=np.float32, crossing=0.3, vl=32,
+                 sort=False, cdt=(0.45, 0.40, 0.35), qdt_2mc=-0.05, edge_cases=True):
+    """Random interpolator + particles on an nx*ny*nz periodic grid.
+
+    A fraction `crossing` of the particles gets large momenta (several face
+    crossings per push); the rest move within their cell.  With edge_cases,
+    some particles sit exactly on faces or have zero momentum components."""
+    R = np.dtype(real).type
+    rng = np.random.default_rng(seed)
+    sx, sy, sz = nx + 2, ny + 2, nz + 2
+    num_cells = sx * sy * sz
+    # interpolator coefficients for every cell (ghost cells are never gathered)
+    scale = np.array([0.2, 0.05, 0.05, 0.01] * 3 + [0.8, 0.1] * 3)
+    interp_vals = (rng.standard_normal((num_cells, 18)) * scale).astype(R)
+    interp = L.pack_cells(interp_vals, R)
+    ix = rng.integers(1, nx + 1, n)
+    iy = rng.integers(1, ny + 1, n)
+    iz = rng.integers(1, nz + 1, n)
+    cell = L.voxel(ix, iy, iz, nx, ny).astype(np.int32)
+    off = rng.uniform(-1, 1, (3, n))
+    big = rng.random(n) < crossing
+    u = rng.standard_normal((3, n)) * np.where(big, 3.0, 0.004)
+    if edge_cases and n >= 64:
+        k = n // 16
+        off[0, :k] = 1.0            # on the +x face, moving in or out
+        off[1, k:2 * k] = -1.0      # on the -y face
+        u[2, 2 * k:3 * k] = 0.0     # zero z motion (the 3.4e38 sentinel)
+        u[:, 3 * k:3 * k + 8] = 0.0  # at rest
+    w = rng.uniform(0.5, 1.5, n)
+    p = dict(x=off[0], y=off[1], z=off[2], ux=u[0], uy=u[1], uz=u[2], w=w, cell=cell)
+    if sort:
+        order = np.argsort(cell, kind="stable")
+        p = {k: v[order] for k, v in p.items()}
+    p = {k: (v.astype(R) if k != "cell" else v) for k, v in p.items()}
+    packed = L.pack_particles(p, R, vl)
+    push_args = (R(qdt_2mc), R(cdt[0]), R(cdt[1]), R(cdt[2]), R(-1.0))
+    return dict(particles=packed, host=p, interp=interp, interp_vals=interp_vals,
+                push_args=push_args, ogrid=oracle.Oracle.grid(nx, ny, nz, 1), nx=nx, ny=ny, nz=nz,
+                n=n, num_cells=num_cells, real=np.dtype(real), vl=vl)
+
+
+def random_fields(nx, ny, nz, seed=0, real=np.float32, scale=1.0):
+    """Random values for all 9 field members of every cell (AoSoA, flat)."""
+    rng = np.random.default_rng(seed)
+    nc = (nx + 2) * (ny + 2) * (nz + 2)
+    vals = (rng.standard_normal((nc, 9)) * scale).astype(real)
+    return L.pack_cells(vals, real), nc
+
+
+def reorder_bound(acc_abs, count, eps):
+    """Bound on |sum_a - sum_b| for two summation orders of the same terms:
+    2 (k-1) eps sum|x| per accumulator (recursive summation error bound)."""
+    k = np.maximum(count.astype(np.float64) - 1, 0)
+    return 2.0 * k * eps * acc_abs.astype(np.float64) + 1e-30

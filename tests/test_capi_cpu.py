@@ -1,0 +1,112 @@
+"""CPU-side checks of the C-ABI library: it loads, exports every entry point
+that include/cpic/capi.h declares, and rejects bad arguments before any CUDA
+call (so these run without a GPU)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "cpic", "capi.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(cpic_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cabanapic_gb300 import build, capi
+    build.build()
+    return capi.load()
+
+
+def test_header_declares_the_expected_entry_points():
+    names = _declared()
+    for must in ("cpic_push", "cpic_load_interpolator", "cpic_unload_accumulator",
+                 "cpic_clear_accumulator", "cpic_advance_b", "cpic_advance_e",
+                 "cpic_field_energies", "cpic_sort_particles", "cpic_status_read"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in _declared() if not hasattr(lib.dll, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_the_header(lib):
+    from cabanapic_gb300 import capi
+    assert set(_declared()) <= set(capi.exported_symbols())
+
+
+def test_version_and_strerror(lib):
+    assert lib.dll.cpic_version() >= 1
+    assert lib.dll.cpic_strerror(-2).decode().startswith("unsupported")
+    assert lib.dll.cpic_strerror(12345).decode() == "unknown cpic error"
+
+
+def _prm(**kw):
+    from cabanapic_gb300 import capi
+    d = dict(qdt_2mc=-0.01, cdt_dx=0.5, cdt_dy=0.5, cdt_dz=0.5, qsp=-1.0, precision=4,
+             particle_vl=32, flags=0, reserved=0)
+    d.update(kw)
+    return capi.CpicPushParams(**d)
+
+
+def test_push_argument_validation(lib):
+    from cabanapic_gb300 import capi
+    push = lib.raw("cpic_push")
+    g = capi.make_grid(4, 4, 4)
+    status = C.c_int32(0)
+    dummy = C.c_void_p(64)  # never dereferenced: validation fails first
+    assert push(dummy, 10, dummy, dummy, None, C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(dummy, 10, dummy, dummy, C.byref(g), None, C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(precision=2)), C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(particle_vl=8)), C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(flags=8)), C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(None, 10, dummy, dummy, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(dummy, -1, dummy, dummy, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    # empty particle list: nothing to do, no device access
+    assert push(None, 0, None, None, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_OK
+    refl = capi.make_grid(4, 4, 4, 1, capi.CPIC_REFLECT)
+    assert push(dummy, 10, dummy, dummy, C.byref(refl), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EUNSUPPORTED
+    ng2 = capi.make_grid(4, 4, 4, 2)
+    assert push(dummy, 10, dummy, dummy, C.byref(ng2), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EUNSUPPORTED
+    bad = capi.make_grid(0, 4, 4)
+    assert push(dummy, 10, dummy, dummy, C.byref(bad), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    # misaligned accumulator (vector reductions need 16-byte alignment)
+    assert push(dummy, 10, dummy, C.c_void_p(68), C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+
+
+def test_field_argument_validation(lib):
+    from cabanapic_gb300 import capi
+    g = capi.make_grid(4, 4, 4)
+    d = C.c_void_p(64)
+    assert lib.raw("cpic_load_interpolator")(None, d, C.byref(g), 4, None) == capi.CPIC_EINVAL
+    assert lib.raw("cpic_load_interpolator")(d, d, C.byref(g), 3, None) == capi.CPIC_EINVAL
+    assert lib.raw("cpic_advance_b")(d, 0.1, 0.1, 0.1, C.byref(capi.make_grid(4, 4, 4, 1, 0)), 4, None) == capi.CPIC_EUNSUPPORTED
+    assert lib.raw("cpic_advance_e")(None, 0.1, 0.1, 0.1, C.byref(g), 0.1, 4, None) == capi.CPIC_EINVAL
+    assert lib.raw("cpic_unload_accumulator")(d, None, C.byref(g), 1.0, 1.0, 1.0, 1.0, 4, None) == capi.CPIC_EINVAL
+    assert lib.raw("cpic_field_energies")(d, C.byref(g), 4, d, d, 8, None) == capi.CPIC_ESCRATCH
+    assert lib.raw("cpic_energy_scratch_bytes")() > 0
+
+
+def test_sort_scratch_query(lib):
+    q = lib.raw("cpic_sort_scratch_bytes")
+    from cabanapic_gb300 import layout as L
+    n, nc = 100000, 5000
+    b = q(n, nc, 4, 32)
+    assert b >= L.particle_list_bytes(n, np.float32, 32) + 8 * n + 4 * nc
+    assert q(n, nc, 3, 32) == 0 and q(n, nc, 4, 7) == 0 and q(-1, nc, 4, 32) == 0
+
+
+def test_no_allocation_calls_in_library_sources():
+    """The library allocates nothing: scratch comes from the caller."""
+    csrc = os.path.join(ROOT, "cabanapic_gb300", "csrc")
+    for f in os.listdir(csrc):
+        if f.endswith(".cu"):
+            s = open(os.path.join(csrc, f)).read()
+            assert "cudaMalloc" not in s and "cudaFree" not in s, f

@@ -1,0 +1,85 @@
+"""Host-side layout packing and deck arithmetic, checked against the oracle."""
+import numpy as np
+import pytest
+
+from cabanapic_gb300 import decks, layout as L
+
+
+@pytest.mark.parametrize("real,vl", [(np.float32, 32), (np.float32, 16), (np.float64, 32), (np.float64, 16)])
+def test_particle_pack_roundtrip(real, vl):
+    rng = np.random.default_rng(1)
+    n = 1000 + vl // 2
+    p = {k: rng.standard_normal(n).astype(real) for k in L.PARTICLE_REAL_MEMBERS}
+    p["cell"] = rng.integers(0, 1 << 20, n).astype(np.int32)
+    buf = L.pack_particles(p, real, vl)
+    assert buf.nbytes == L.particle_list_bytes(n, real, vl)
+    q = L.unpack_particles(buf, n, real, vl)
+    for k in p:
+        assert np.array_equal(p[k], q[k])
+    # member m of particle i sits at (i//vl)*block + m*vl*rs + (i%vl)*rs
+    rs = np.dtype(real).itemsize
+    i = 777
+    off = (i // vl) * L.particle_block_bytes(real, vl) + 3 * vl * rs + (i % vl) * rs
+    assert buf[off:off + rs].view(real)[0] == p["ux"][i]
+    off = (i // vl) * L.particle_block_bytes(real, vl) + 7 * vl * rs + (i % vl) * 4
+    assert buf[off:off + 4].view(np.int32)[0] == p["cell"][i]
+
+
+def test_cell_pack_roundtrip():
+    rng = np.random.default_rng(2)
+    v = rng.standard_normal((1001, 18)).astype(np.float32)
+    a = L.pack_cells(v, np.float32)
+    assert a.size == L.cell_array_bytes(1001, 18, np.float32) // 4
+    assert np.array_equal(L.unpack_cells(a, 1001, 18), v)
+    c, m = 555, 13
+    assert a[(c // 32) * 18 * 32 + m * 32 + c % 32] == v[c, m]
+
+
+def test_voxel_and_rank_to_index():
+    nx, ny, nz = 7, 5, 3
+    x, y, z = np.meshgrid(np.arange(nx + 2), np.arange(ny + 2), np.arange(nz + 2), indexing="ij")
+    c = L.voxel(x, y, z, nx, ny)
+    assert c.max() == (nx + 2) * (ny + 2) * (nz + 2) - 1
+    ix, iy, iz = L.rank_to_index(c, nx, ny)
+    assert np.array_equal(ix, x) and np.array_equal(iy, y) and np.array_equal(iz, z)
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_two_stream_em_deck_matches_oracle(orc, prec):
+    d = decks.two_stream_em(prec)
+    p = d.derived()
+    _, par = orc.run_two_stream_em(1, prec)
+    for k in ("dt", "dx", "dy", "dz", "qdt_2mc", "we", "py"):
+        assert float(p[k]) == par[k], k
+    assert float(p["len_y"]) == par["len_y"]
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_default_initializer_matches_oracle_bitwise(orc, prec):
+    d = decks.two_stream_em(prec)
+    p = d.derived()
+    R = d.R
+    buf = L.pack_particles(decks.default_particles(d), R, 32)
+    ref = np.zeros_like(buf)
+    orc.default_particle_init(ref, d.num_particles, 32, d.nx, d.ny, p["dxp"], d.nppc, p["we"], R(d.v0), R)
+    assert np.array_equal(buf, ref)
+
+
+def test_thermal_initializer_shapes():
+    d = decks.thermal(n=4, ppc=8, num_steps=1)
+    p = decks.thermal_particles(d)
+    assert len(p["cell"]) == 4 ** 3 * 8
+    assert np.all(np.diff(p["cell"]) >= 0)  # cell order
+    assert np.abs(p["x"]).max() <= 1 and np.abs(p["y"]).max() <= 1
+    ix, iy, iz = L.rank_to_index(p["cell"], 4, 4)
+    assert ix.min() == 1 and ix.max() == 4 and iz.max() == 4
+    np.testing.assert_allclose(p["w"].sum(), 1.0 * d.len_x_global ** 3, rtol=1e-5)
+    buf = decks.thermal_particles(d, packed=True)
+    assert np.array_equal(L.unpack_particles(buf, len(p["cell"]))["ux"], p["ux"])
+
+
+def test_courant_length():
+    R = np.float32
+    cl = decks.courant_length(1.0, 2.0, 3.0, 10, 20, 30, R)
+    w = (10 / 1.0) ** 2 + (20 / 2.0) ** 2 + (30 / 3.0) ** 2
+    assert abs(float(cl) - (1 / w) ** 0.5) < 1e-7

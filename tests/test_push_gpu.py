@@ -1,0 +1,97 @@
+"""Parity of the GPU push (cpic_push through the C ABI) against the oracle.
+
+Particle state (offsets, momenta, cell index) must be bit-identical: the
+kernel and the oracle perform the reference's arithmetic in the same order
+with separately rounded operations.  Accumulators are sums of the same terms
+in a different order (warp reductions and atomics), so they must agree within
+the recursive-summation bound 2 (k-1) eps sum|x| per accumulator.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from support import random_state, reorder_bound  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_pair(orc, st, true_sqrt=False):
+    from cabanapic_gb300 import pic
+    R = st["real"]
+    nc = st["num_cells"]
+    host = st["particles"].copy()
+    acc = np.zeros((nc, 3, 4), R)
+    acc_abs = np.zeros((nc, 3, 4), R)
+    cnt = np.zeros((nc, 3, 4), np.int32)
+    crossers = orc.push(host, st["n"], st["vl"], st["interp"], *st["push_args"], acc, st["ogrid"],
+                        acc_abs=acc_abs, acc_count=cnt, literal=not true_sqrt)
+    P = pic.ParticleList(st["n"], R, st["vl"]).upload(st["particles"])
+    I = pic.InterpolatorArray(nc, R)
+    I.buf.copy_(torch.from_numpy(st["interp"]))
+    A = pic.AccumulatorArray(nc, R)
+    pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic,
+             true_sqrt=true_sqrt)
+    pic.check_status()
+    return host, acc, acc_abs, cnt, P.download_bytes(), A.get(), crossers
+
+
+def _assert_parity(res, real):
+    host, acc, acc_abs, cnt, gpu_p, gpu_acc, _ = res
+    assert np.array_equal(gpu_p, host), "particle AoSoA bytes differ from the oracle"
+    eps = np.finfo(real).eps
+    bound = reorder_bound(acc_abs, cnt, eps)
+    err = np.abs(gpu_acc.astype(np.float64) - acc.astype(np.float64))
+    assert np.all(err <= bound), f"accumulator error {err.max():.3e} above the reordering bound"
+
+
+@pytest.mark.parametrize("sort", [False, True])
+@pytest.mark.parametrize("n", [1, 31, 4000, 20011])
+def test_push_float_vl32(orc, sort, n):
+    st = random_state(nx=6, ny=5, nz=4, n=n, seed=n + int(sort), sort=sort)
+    res = _run_pair(orc, st)
+    _assert_parity(res, np.float32)
+    if n >= 4000:
+        assert res[-1] > 0.2 * n  # the crossing path was exercised
+
+
+def test_push_float_vl16(orc):
+    st = random_state(nx=5, ny=4, nz=6, n=9999, seed=3, vl=16)
+    _assert_parity(_run_pair(orc, st), np.float32)
+
+
+@pytest.mark.parametrize("true_sqrt", [False, True])
+def test_push_double(orc, true_sqrt):
+    st = random_state(nx=4, ny=6, nz=5, n=6007, seed=11, real=np.float64)
+    _assert_parity(_run_pair(orc, st, true_sqrt=true_sqrt), np.float64)
+
+
+def test_push_collapsed_axes(orc):
+    # a 1-D grid (ny = nz = 1), like the reference's 2stream decks
+    st = random_state(nx=32, ny=1, nz=1, n=5000, seed=5, cdt=(0.5, 0.2, 0.2))
+    _assert_parity(_run_pair(orc, st), np.float32)
+
+
+def test_push_dense_cells_sorted(orc):
+    # 64+ particles per cell in cell order: the warp-reduction path dominates
+    st = random_state(nx=4, ny=4, nz=4, n=64 * 64 + 17, seed=9, sort=True, crossing=0.05)
+    _assert_parity(_run_pair(orc, st), np.float32)
+
+
+def test_push_accumulates_into_existing_values(orc):
+    # push adds to the accumulator (ScatterView semantics): a non-zero start is kept
+    from cabanapic_gb300 import pic
+    st = random_state(n=3000, seed=21)
+    nc = st["num_cells"]
+    start = np.random.default_rng(0).standard_normal((nc, 3, 4)).astype(np.float32)
+    host = st["particles"].copy()
+    acc = start.copy()
+    orc.push(host, st["n"], 32, st["interp"], *st["push_args"], acc, st["ogrid"])
+    P = pic.ParticleList(st["n"], np.float32, 32).upload(st["particles"])
+    I = pic.InterpolatorArray(nc, np.float32)
+    I.buf.copy_(torch.from_numpy(st["interp"]))
+    A = pic.AccumulatorArray(nc, np.float32)
+    A.set(start)
+    pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic)
+    pic.check_status()
+    assert np.allclose(A.get(), acc, rtol=1e-5, atol=1e-5)
