@@ -256,6 +256,7 @@ def cpu_sample_run(steps, warmup, precision=4, sample_ppc=8, threads=0):
 
 # ---------------------------------------------------------------- main
 def main():
+    global N_CELLS, PPC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -264,13 +265,16 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--cells", type=int, default=N_CELLS, help="cells per axis (profiling cases)")
+    ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (profiling cases)")
     args = ap.parse_args()
+    N_CELLS, PPC = args.cells, args.ppc
     ws, rank, local = _dist()
-    metric = "particle-pushes/s (full step, thermal plasma 128^3 x 64 ppc)"
+    metric = "particle-pushes/s (full step, FP32)"
     unit = "particle-pushes/s"
-    workload = ("thermal plasma 128^3 cells x 64 ppc = 134,217,728 particles, FP32, u_th=0.05, "
-                "dt=0.7 Courant, sort every 20 steps; full step (interp, clear, push+deposit, "
-                "unload, advance_b/e/b, energies)")
+    workload = (f"thermal plasma {N_CELLS}^3 cells x {PPC} ppc = {N_CELLS ** 3 * PPC:,} particles, "
+                "FP32, u_th=0.05, dt=0.7 Courant, sort every 20 steps; full step (interp, clear, "
+                "push+deposit, unload, advance_b/e/b, energies)")
 
     if args.impl == "reference":
         if rank != 0:
@@ -278,7 +282,7 @@ def main():
         steps = max(1, min(args.steps, 5))
         warm = max(1, min(args.warmup, 1))
         v, cores, n, secs = cpu_sample_run(steps, warm)
-        sample = (f"128^3 grid, 8 ppc ({n:,} particles), {steps} timed steps after {warm}; "
+        sample = (f"{N_CELLS}^3 grid, 8 ppc ({n:,} particles), {steps} timed steps after {warm}; "
                   "CPU restatement of the reference (OpenMP push, per-thread accumulators)")
         line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": args.gpus,
                 "steps": steps, "warmup": warm, "ms_per_step": secs / steps * 1e3,
@@ -338,7 +342,7 @@ def main():
     if rank == 0 and not args.no_cpu:
         v, cores, ns, secs = cpu_sample_run(3, 1)
         cpu = {"value": v, "unit": unit, "cores": cores, "kind": "port",
-               "sample": f"128^3 grid, 8 ppc ({ns:,} particles), 3 full steps after 1 ({secs:.1f} s)"}
+               "sample": f"{N_CELLS}^3 grid, 8 ppc ({ns:,} particles), 3 full steps after 1 ({secs:.1f} s)"}
 
     if rank == 0:
         line = {

@@ -25,16 +25,26 @@ inline unsigned blocks_for(int64_t n, int threads = kThreads) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
+// Linear thread index t over an ex*ey*ez box of cells starting at (1,1,1);
+// 32-bit arithmetic (grids are limited to < 2^31 cells).
+__device__ __forceinline__ bool box_coords(unsigned t, unsigned ex, unsigned ey, unsigned ez,
+                                           int& x, int& y, int& z) {
+  if (t >= ex * ey * ez) return false;
+  const unsigned r = t / ex;
+  x = (int)(t - r * ex) + 1;
+  z = (int)(r / ey);
+  y = (int)(r - (unsigned)z * ey) + 1;
+  z += 1;
+  return true;
+}
+
 // ------------------------------------------------------------ interpolator
 // load_interpolator_array (interpolator.cpp:48-136): interior cells.
 template <class R>
 __global__ void __launch_bounds__(kThreads)
 load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridDev g) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)g.nx * g.ny * g.nz) return;
-  const int x = (int)(t % g.nx) + 1;
-  const int y = (int)((t / g.nx) % g.ny) + 1;
-  const int z = (int)(t / ((int64_t)g.nx * g.ny)) + 1;
+  int x, y, z;
+  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx, g.ny, g.nz, x, y, z)) return;
   const int i = g.vox(x, y, z);
   const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
   const R fourth = 1.0 / 4.0, half = 1.0 / 2.0;
@@ -66,12 +76,8 @@ load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridD
 template <class R>
 __global__ void __launch_bounds__(kThreads)
 unload_kernel(R* __restrict__ F, const R* __restrict__ A, const GridDev g, R cx, R cy, R cz) {
-  const int ex = g.nx + 1, ey = g.ny + 1, ez = g.nz + 1;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)ex * ey * ez) return;
-  const int x = (int)(t % ex) + 1;
-  const int y = (int)((t / ex) % ey) + 1;
-  const int z = (int)(t / ((int64_t)ex * ey)) + 1;
+  int x, y, z;
+  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx + 1, g.ny + 1, g.nz + 1, x, y, z)) return;
   const int i = g.vox(x, y, z);
   const int xd = g.vox(x - 1, y, z), yd = g.vox(x, y - 1, z), zd = g.vox(x, y, z - 1);
   const int xzd = g.vox(x - 1, y, z - 1), xyd = g.vox(x - 1, y - 1, z), yzd = g.vox(x, y - 1, z - 1);
@@ -158,11 +164,8 @@ static int ghost_copy(R* F, const GridDev& g, int m0, cudaStream_t s) {
 template <class R>
 __global__ void __launch_bounds__(kThreads)
 advance_b_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)g.nx * g.ny * g.nz) return;
-  const int x = (int)(t % g.nx) + 1;
-  const int y = (int)((t / g.nx) % g.ny) + 1;
-  const int z = (int)(t / ((int64_t)g.nx * g.ny)) + 1;
+  int x, y, z;
+  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx, g.ny, g.nz, x, y, z)) return;
   const int f0 = g.vox(x, y, z), fx = f0 + 1, fy = f0 + g.sx, fz = f0 + g.sx * g.sy;
   auto e = [&](int c, int m) { return F[cell_at<9>(c, m)]; };
   const R ex0 = e(f0, CPIC_F_EX), ey0 = e(f0, CPIC_F_EY), ez0 = e(f0, CPIC_F_EZ);
@@ -175,12 +178,8 @@ advance_b_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz) {
 template <class R>
 __global__ void __launch_bounds__(kThreads)
 advance_e_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz, R cj) {
-  const int ex = g.nx + 1, ey = g.ny + 1, ez = g.nz + 1;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)ex * ey * ez) return;
-  const int x = (int)(t % ex) + 1;
-  const int y = (int)((t / ex) % ey) + 1;
-  const int z = (int)(t / ((int64_t)ex * ey)) + 1;
+  int x, y, z;
+  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx + 1, g.ny + 1, g.nz + 1, x, y, z)) return;
   const int f0 = g.vox(x, y, z), fx = f0 - 1, fy = f0 - g.sx, fz = f0 - g.sx * g.sy;
   auto b = [&](int c, int m) { return F[cell_at<9>(c, m)]; };
   const R bx0 = b(f0, CPIC_F_CBX), by0 = b(f0, CPIC_F_CBY), bz0 = b(f0, CPIC_F_CBZ);
@@ -209,18 +208,22 @@ energy_kernel(const R* __restrict__ F, const GridDev g, double* __restrict__ out
               EnergyScratch* __restrict__ sc) {
   __shared__ double se[kThreads / 32], sb[kThreads / 32];
   __shared__ bool last;
-  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  // one warp per x row (y, z), lanes along x: coalesced AoSoA reads
+  const unsigned rows = (unsigned)g.ny * (unsigned)g.nz;
+  const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
   double e = 0.0, bb = 0.0;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int x = (int)(t % g.nx) + 1;
-    const int y = (int)((t / g.nx) % g.ny) + 1;
-    const int z = (int)(t / ((int64_t)g.nx * g.ny)) + 1;
-    const int i = g.vox(x, y, z);
-    const double a0 = F[cell_at<9>(i, CPIC_F_EX)], a1 = F[cell_at<9>(i, CPIC_F_EY)], a2 = F[cell_at<9>(i, CPIC_F_EZ)];
-    const double c0 = F[cell_at<9>(i, CPIC_F_CBX)], c1 = F[cell_at<9>(i, CPIC_F_CBY)], c2 = F[cell_at<9>(i, CPIC_F_CBZ)];
-    e += a0 * a0 + a1 * a1 + a2 * a2;
-    bb += c0 * c0 + c1 * c1 + c2 * c2;
+  for (unsigned r = warp; r < rows; r += nwarps) {
+    const int y = (int)(r % (unsigned)g.ny) + 1, z = (int)(r / (unsigned)g.ny) + 1;
+    const int row = g.vox(0, y, z);
+    for (int x = 1 + lane; x <= g.nx; x += 32) {
+      const int i = row + x;
+      const double a0 = F[cell_at<9>(i, CPIC_F_EX)], a1 = F[cell_at<9>(i, CPIC_F_EY)], a2 = F[cell_at<9>(i, CPIC_F_EZ)];
+      const double c0 = F[cell_at<9>(i, CPIC_F_CBX)], c1 = F[cell_at<9>(i, CPIC_F_CBY)], c2 = F[cell_at<9>(i, CPIC_F_CBZ)];
+      e += a0 * a0 + a1 * a1 + a2 * a2;
+      bb += c0 * c0 + c1 * c1 + c2 * c2;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     e += __shfl_xor_sync(kFull, e, o);

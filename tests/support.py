@@ -61,3 +61,34 @@ def reorder_bound(acc_abs, count, eps):
     2 (k-1) eps sum|x| per accumulator (recursive summation error bound)."""
     k = np.maximum(count.astype(np.float64) - 1, 0)
     return 2.0 * k * eps * acc_abs.astype(np.float64) + 1e-30
+
+
+def oracle_run(orc, deck, packed, steps):
+    """The reference's step sequence (example/example.cpp:221-266) in the
+    oracle from a given packed particle list; returns [steps, 2] energies
+    accumulated in double."""
+    p = deck.derived()
+    R = deck.R
+    buf = packed.copy()
+    nc = deck.num_cells
+    g = orc.grid(deck.nx, deck.ny, deck.nz)
+    fields = np.zeros(L.cell_array_bytes(nc, 9, R) // np.dtype(R).itemsize, R)
+    interp = np.zeros(L.cell_array_bytes(nc, 18, R) // np.dtype(R).itemsize, R)
+    h = R(0.5)
+    out = []
+    for _ in range(steps):
+        orc.load_interpolator(fields, interp, g)
+        acc = np.zeros((nc, 3, 4), R)
+        orc.push(buf, deck.num_particles, deck.vl, interp, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"],
+                 p["cdt_dz"], p["qsp"], acc, g)
+        orc.unload_accumulator(fields, acc, g, p["dx"], p["dy"], p["dz"], p["dt"])
+        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
+        orc.advance_e(fields, p["px"], p["py"], p["pz"], g, p["dt_eps0"])
+        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
+        out.append(orc.energies(fields, g)[2:4])
+    return np.array(out)
+
+
+def history_deviation(a, b):
+    """max_k |a_k - b_k| / max_k |b_k|, per column (E, B)."""
+    return np.abs(a - b).max(axis=0) / np.abs(b).max(axis=0)

@@ -10,6 +10,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from conftest import gold_path  # noqa: E402
+from support import history_deviation, oracle_run  # noqa: E402
 from oracle import energy_rule  # noqa: E402
 
 pytestmark = pytest.mark.gpu
@@ -37,22 +38,58 @@ def test_double_gpu_reproduces_double_gold(gpu_runs):
     assert rel.max() < 2e-6, rel.max()
 
 
-@pytest.mark.parametrize("prec,kind", [(4, "float"), (8, "double")])
-def test_gpu_passes_reference_acceptance_rule(gpu_runs, prec, kind):
-    e, p = gpu_runs[prec]
+def test_gpu_passes_reference_acceptance_rule(gpu_runs):
+    """The reference's regression rule, applied as its CI applies it: to the
+    real_t=double build (CI.yml builds REAL_TYPE=double).  In FP32 the run is
+    chaotic in the checked window (rows 3581-4880): the reference's own float
+    and double golds differ there by up to 110% in E, so the float result
+    depends on the summation order and is checked in the linear phase below."""
+    e, p = gpu_runs[8]
     ours = energy_rule.format_history(e, float(p["dt"]))
-    gold = open(gold_path(kind)).read().splitlines()
+    gold = open(gold_path("double")).read().splitlines()
     (e_ok, e_err, _, _), (b_ok, b_err, _, _) = energy_rule.two_stream_em_check(gold, ours)
     assert e_ok, e_err
     assert b_ok, b_err
 
 
-def test_float_gpu_tracks_oracle_early(gpu_runs, orc):
-    e, _ = gpu_runs[4]
-    ref, _ = orc.run_two_stream_em(200, 4)
-    rel = np.abs(e[:200] / ref[:, 2:4] - 1)
-    assert rel[:50].max() < 1e-5, rel[:50].max()
-    assert rel.max() < 1e-3, rel.max()
+def test_float_gpu_within_reordering_envelope(gpu_runs, orc):
+    """In FP32 the counter-streaming beams' currents cancel to ~1e-4 of the
+    individual deposits, so the summation order of the deposit alone moves the
+    energy history at the 1e-4 level.  The oracle run on randomly permuted
+    particle orders (identical particles, different accumulation order) gives
+    that envelope; the GPU's atomics must stay within a small multiple of it."""
+    from cabanapic_gb300 import decks, layout as L
+    deck = decks.two_stream_em(precision=4, num_steps=200)
+    host = decks.default_particles(deck)
+    base = oracle_run(orc, deck, L.pack_particles(host, np.float32, 32), 200)
+    rng = np.random.default_rng(0)
+    env = np.zeros(2)
+    for _ in range(4):
+        perm = rng.permutation(deck.num_particles)
+        ph = {k: v[perm] for k, v in host.items()}
+        e = oracle_run(orc, deck, L.pack_particles(ph, np.float32, 32), 200)
+        env = np.maximum(env, history_deviation(e, base))
+    gpu = gpu_runs[4][0][:200]
+    dev = history_deviation(gpu, base)
+    assert np.all(env > 0)
+    assert np.all(dev <= 3 * env), (dev, env)
+
+
+def test_float_gpu_error_against_fp64_truth_in_linear_phase(gpu_runs, orc):
+    """FP32 versus the FP64 oracle over the first 300 steps: the GPU's error
+    is the FP32 algorithm's error (the FP32 oracle's own), not more."""
+    e32, _ = gpu_runs[4]
+    truth, _ = orc.run_two_stream_em(300, 8)
+    own, _ = orc.run_two_stream_em(300, 4)
+    dev_gpu = history_deviation(e32[:300], truth[:, 2:4])
+    dev_orc = history_deviation(own[:, 2:4], truth[:, 2:4])
+    assert np.all(dev_gpu <= 2 * dev_orc + 1e-4), (dev_gpu, dev_orc)
+
+
+def test_double_gpu_tracks_double_oracle(gpu_runs, orc):
+    e, _ = gpu_runs[8]
+    ref, _ = orc.run_two_stream_em(1000, 8)
+    assert np.all(history_deviation(e[:1000], ref[:, 2:4]) < 1e-9)
 
 
 def test_thermal_3d_steps_track_oracle(orc):
@@ -67,44 +104,43 @@ def test_thermal_3d_steps_track_oracle(orc):
     sim.run(20)
     sim.check_status()
     e_gpu = sim.energies()
-    # oracle, same sequence
-    R = deck.R
-    buf = L.pack_particles(host, R, 32)
-    nc = deck.num_cells
-    g = orc.grid(deck.nx, deck.ny, deck.nz)
-    fields = np.zeros(L.cell_array_bytes(nc, 9, R) // R().itemsize, R)
-    interp = np.zeros(L.cell_array_bytes(nc, 18, R) // R().itemsize, R)
-    e_ref = []
-    for _ in range(20):
-        orc.load_interpolator(fields, interp, g)
-        acc = np.zeros((nc, 3, 4), R)
-        orc.push(buf, deck.num_particles, 32, interp, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"],
-                 p["cdt_dz"], p["qsp"], acc, g)
-        orc.unload_accumulator(fields, acc, g, p["dx"], p["dy"], p["dz"], p["dt"])
-        h = R(0.5)
-        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
-        orc.advance_e(fields, p["px"], p["py"], p["pz"], g, p["dt_eps0"])
-        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
-        e_ref.append(orc.energies(fields, g)[2:4])
-    e_ref = np.array(e_ref)
+    e_ref = oracle_run(orc, deck, L.pack_particles(host, deck.R, 32), 20)
     rel = np.abs(e_gpu / e_ref - 1)
     assert rel.max() < 1e-4, rel.max()
 
 
-@pytest.mark.parametrize("exe,kind", [("minipic", "float"), ("minipic_f64", "double")])
-def test_cpp_driver_passes_reference_rule(tmp_path, exe, kind):
-    """The C++ time loop written against include/cpic/cabana.hpp (the
-    reference's push() signature and containers) runs the 2stream-em deck and
-    its energies.txt passes the reference's regression rule."""
+def _run_minipic(tmp_path, exe, steps):
     from cabanapic_gb300 import build
     path = os.path.join(build.OUT, exe)
     assert os.path.exists(path), "C++ driver not built"
     out = tmp_path / "energies.txt"
-    r = subprocess.run([path, "6000", str(out)], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([path, str(steps), str(out)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
-    ours = out.read_text().splitlines()
-    assert len(ours) == 6000
-    gold = open(gold_path(kind)).read().splitlines()
+    lines = out.read_text().splitlines()
+    assert len(lines) == steps
+    return lines
+
+
+def test_cpp_driver_passes_reference_rule(tmp_path):
+    """The C++ time loop written against include/cpic/cabana.hpp (the
+    reference's push() signature and containers) runs the 2stream-em deck in
+    double and its energies.txt passes the reference's regression rule."""
+    ours = _run_minipic(tmp_path, "minipic_f64", 6000)
+    gold = open(gold_path("double")).read().splitlines()
     (e_ok, e_err, _, _), (b_ok, b_err, _, _) = energy_rule.two_stream_em_check(gold, ours)
     assert e_ok, e_err
     assert b_ok, b_err
+    g = np.loadtxt(gold_path("double"))
+    mine = np.array([[float(t) for t in l.split()] for l in ours])
+    assert np.abs(mine[:, 2:4] / g[:, 2:4] - 1).max() < 2e-5  # ostream prints 6 digits
+
+
+def test_cpp_driver_float(tmp_path, orc):
+    """The real_t=float C++ driver: the linear phase matches the FP32 error
+    level against the FP64 oracle."""
+    ours = _run_minipic(tmp_path, "minipic", 300)
+    mine = np.array([[float(t) for t in l.split()] for l in ours])[:, 2:4]
+    truth, _ = orc.run_two_stream_em(300, 8)
+    own, _ = orc.run_two_stream_em(300, 4)
+    assert np.all(history_deviation(mine, truth[:, 2:4]) <=
+                  2 * history_deviation(own[:, 2:4], truth[:, 2:4]) + 1e-4)
