@@ -81,6 +81,7 @@ _SIGS = {
     "cpic_advance_e": (_i32, [_vp, _f64, _f64, _f64, C.POINTER(CpicGrid), _f64, _i32, _vp]),
     "cpic_energy_scratch_bytes": (_sz, []),
     "cpic_field_energies": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _vp, _vp, _sz, _vp]),
+    "cpic_field_energies_noalloc": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _vp, _vp]),
     "cpic_sort_scratch_bytes": (_sz, [_i64, _i64, _i32, _i32]),
     "cpic_sort_particles": (_i32, [_vp, _i64, _i64, _i32, _i32, _vp, _sz, _vp]),
     "cpic_status_clear": (_i32, [_vp, _vp]),

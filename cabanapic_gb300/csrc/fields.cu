@@ -14,6 +14,8 @@
 // fixed reduction tree, so it is deterministic.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "common.cuh"
 
 namespace cpic {
@@ -425,6 +427,58 @@ extern "C" int cpic_field_energies(const void* fields, const cpic_grid* grid, in
   const GridDev g = make_grid(grid);
   return precision == CPIC_FLOAT ? typed_energies<float>(fields, g, d_out, d_scratch, s)
                                  : typed_energies<double>(fields, g, d_out, d_scratch, s);
+}
+
+// ------------------------------------------------------------ energies without allocation
+// Some callers cannot allocate device memory: a host code whose device memory
+// is all owned by its own pool or arena, a language binding that has no CUDA
+// runtime allocator to call, or a per-step diagnostic that must not allocate
+// in the middle of a time loop.  cpic_field_energies_noalloc serves them: the
+// energy reduction's scratch (one partial sum pair per block of the fixed
+// 592-block launch, plus the completion counter: 9,480 bytes) lives in the
+// static device array below.  Every GPU that loads this library holds the
+// array until the process exits.
+static_assert(sizeof(EnergyScratch) == 9480, "static energy scratch size is documented as 9,480 bytes");
+static __device__ __align__(256) EnergyScratch g_energy_noalloc_scratch;
+
+constexpr int kMaxDevices = 64;
+// Device address of g_energy_noalloc_scratch per device.  The array's name in
+// host code is only a host-side stand-in, so the address is looked up once per
+// device (by the first call on that device, with it current).
+static std::atomic<EnergyScratch*> g_energy_noalloc_addr[kMaxDevices];
+
+static EnergyScratch* energy_noalloc_scratch() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  EnergyScratch* p = g_energy_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (p == nullptr) {
+    void* addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_energy_noalloc_scratch) != cudaSuccess || addr == nullptr)
+      return nullptr;
+    p = static_cast<EnergyScratch*>(addr);
+    g_energy_noalloc_addr[dev].store(p, std::memory_order_release);
+  }
+  return p;
+}
+
+extern "C" int cpic_field_energies_noalloc(const void* fields, const cpic_grid* grid,
+                                           int32_t precision, double* d_out,
+                                           cpic_stream_t stream) {
+  // The scratch need is fixed (592 block partials), so every grid the library
+  // accepts fits; check_grid rejects the rest (n > 2^20 per axis, >= 2^31 cells).
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields || !d_out) return CPIC_EINVAL;
+  if ((uintptr_t)d_out & 7) return CPIC_EINVAL;
+  EnergyScratch* sc = energy_noalloc_scratch();
+  if (sc == nullptr) return CPIC_ECUDA;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  // the array keeps the previous call's contents: the counter must start at zero
+  if (cudaMemsetAsync(&sc->done, 0, sizeof(unsigned), s) != cudaSuccess) return CPIC_ECUDA;
+  const GridDev g = make_grid(grid);
+  return precision == CPIC_FLOAT ? typed_energies<float>(fields, g, d_out, sc, s)
+                                 : typed_energies<double>(fields, g, d_out, sc, s);
 }
 
 extern "C" int cpic_status_clear(int32_t* d_status, cpic_stream_t stream) {

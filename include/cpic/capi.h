@@ -142,6 +142,21 @@ int cpic_field_energies(const void* fields, const cpic_grid* grid, int32_t preci
                         double* d_out, void* d_scratch, size_t scratch_bytes,
                         cpic_stream_t stream);
 
+/* Energies without allocation -- no counterpart in the reference.  For
+ * callers that cannot allocate device memory (device memory owned by their own
+ * pool or arena, bindings with no CUDA allocator, per-step diagnostics that
+ * must not allocate): the same result as cpic_field_energies, bit for bit, with
+ * the scratch held in a static 9,480-byte device array inside this library
+ * (592 block partial sums and a completion counter; every GPU that loads the
+ * library keeps it until exit).  The scratch need does not grow with the grid;
+ * grids beyond the library's limits (an axis above 2^20 cells, 2^31 ghosted
+ * cells or more) return CPIC_EINVAL.  The first call on a device looks up the
+ * array's device address, so make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (concurrent
+ * streams) race and must be serialised by the caller. */
+int cpic_field_energies_noalloc(const void* fields, const cpic_grid* grid, int32_t precision,
+                                double* d_out, cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- sort
  * Counting sort of the particle list by cell index, in place.  The reference
  * leaves this step commented out (example/example.cpp:226-228, Cabana::sortByKey);
