@@ -136,7 +136,7 @@ def _barrier(ws):
 
 
 # ---------------------------------------------------------------- GPU arm
-def gpu_run(precision, steps, warmup, ws, host_packed=None):
+def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     """Device-resident timed loop; returns dict with times and push events."""
     import torch
     from cabanapic_gb300 import decks
@@ -145,7 +145,8 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None):
     deck = decks.thermal(n=N_CELLS, ppc=PPC, precision=precision, num_steps=steps + warmup)
     if host_packed is None:
         host_packed = decks.thermal_particles(deck, packed=True)
-    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup)
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup,
+                     exact=exact)
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
         sim.step()
@@ -265,6 +266,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-exact", action="store_true")
     ap.add_argument("--cells", type=int, default=N_CELLS, help="cells per axis (profiling cases)")
     ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (profiling cases)")
     args = ap.parse_args()
@@ -319,6 +321,15 @@ def main():
     per_step_launches = 11  # interp, push, unload, 2x(advance_b + ghost copy), fold, ghost copy, advance_e, energies
     launches = args.steps * per_step_launches + 6 * len(range(0, args.steps, SORT_INTERVAL))
 
+    exact = None
+    if not args.no_exact:
+        kx = max(2, min(args.steps, 20))
+        rx, _ = gpu_run(4, kx, max(args.warmup, 3), ws, host_packed, exact=True)
+        msx = _barrier_max(rx["ms"], ws)
+        exact = {"value": n * kx * ws / (msx / 1e3), "ms_per_step": msx / kx, "steps": kx,
+                 "push_ms": float(np.mean(rx["push_ms"])),
+                 "note": "bit-exact push variant (unfused arithmetic, IEEE div/sqrt)"}
+
     e2e = None
     if not args.no_e2e:
         r = e2e_run(4, args.steps, max(args.warmup, 3), host_packed, ws)
@@ -352,10 +363,11 @@ def main():
             "config": {"workload": workload, "particles": n, "cells": deck.num_cells,
                        "l2": "particle list 4.3 GB > L2: no flush needed", "replicas": ws},
             "push_ms": push_ms,
+            "push_ms_by_step": [round(t, 4) for t in res["push_ms"]],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes},
-            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "fp64": fp64,
+            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "fp64": fp64, "exact": exact,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

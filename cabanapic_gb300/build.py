@@ -1,11 +1,13 @@
 """Builds libcpic.so (the CUDA kernels + C ABI) for sm_103a, in-tree.
 
 Each translation unit under csrc/ is compiled by nvcc in parallel, then
-linked into cabanapic_gb300/_build/libcpic.so.  Every unit is built with
---fmad=false: the push and the field stencils then round every multiply and
-add separately, which makes particle states and field values bit-identical to
-a CPU build of the reference compiled without FMA contraction.  IEEE division
-and square root are nvcc's defaults (no --use_fast_math).
+linked into cabanapic_gb300/_build/libcpic.so.  Every unit but push_fast.cu
+is built with --fmad=false: the exact push and the field stencils then round
+every multiply and add separately, which makes particle states and field
+values bit-identical to a CPU build of the reference compiled without FMA
+contraction.  IEEE division and square root are nvcc's defaults (no
+--use_fast_math).  push_fast.cu, the production push, is built with fused
+multiply-adds.
 
 The C++ example driver (csrc/minipic.cpp: the reference's time loop written
 against the C++ push() interface in include/cpic/cabana.hpp) is linked into
@@ -31,7 +33,10 @@ MINIPIC_F64 = os.path.join(OUT, "minipic_f64")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O2", "-I", INCLUDE, "-I", CSRC]
-CU_UNITS = ["push.cu", "fields.cu", "sort.cu"]
+CU_UNITS = ["push.cu", "push_fast.cu", "fields.cu", "sort.cu", "diagnostics.cu", "adjoint_fields.cu",
+            "adjoint_push.cu"]
+# units built with fused multiply-adds (the production push variant)
+FMA_UNITS = {"push_fast.cu"}
 
 
 def _nvcc() -> str:
@@ -67,7 +72,10 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     def compile_one(src):
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
-        log = _run([nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj])
+        flags = list(NVCC_FLAGS)
+        if os.path.basename(src) in FMA_UNITS:
+            flags[flags.index("--fmad=false")] = "--fmad=true"
+        log = _run([nvcc, *ARCH, *flags, *extra, "-c", src, "-o", obj])
         return obj, log
 
     with ThreadPoolExecutor(max_workers=len(CU_UNITS)) as ex:

@@ -26,6 +26,7 @@ CPIC_PERIODIC = 1
 CPIC_FLOAT = 4
 CPIC_DOUBLE = 8
 CPIC_PUSH_TRUE_SQRT = 1
+CPIC_PUSH_EXACT = 2
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -84,6 +85,19 @@ _SIGS = {
     "cpic_field_energies_noalloc": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _vp, _vp]),
     "cpic_sort_scratch_bytes": (_sz, [_i64, _i64, _i32, _i32]),
     "cpic_sort_particles": (_i32, [_vp, _i64, _i64, _i32, _i32, _vp, _sz, _vp]),
+    "cpic_charge_density": (_i32, [_vp, _i64, C.POINTER(CpicGrid), _i32, _i32, _f64, _f64, _f64, _f64,
+                                   _vp, _vp, _vp]),
+    "cpic_diag_scratch_bytes": (_sz, []),
+    "cpic_gauss_residual": (_i32, [_vp, _vp, _vp, _f64, _f64, _f64, _f64, C.POINTER(CpicGrid), _i32,
+                                   _vp, _vp, _vp, _sz, _vp]),
+    "cpic_kinetic_energy": (_i32, [_vp, _i64, _i32, _i32, _f64, _vp, _vp, _sz, _vp]),
+    "cpic_adjoint_push": (_i32, [_vp, _i64, _vp, _vp, _vp, _vp, C.POINTER(CpicGrid),
+                                 C.POINTER(CpicPushParams), _vp, _vp]),
+    "cpic_adjoint_advance_b": (_i32, [_vp, _f64, _f64, _f64, C.POINTER(CpicGrid), _i32, _vp]),
+    "cpic_adjoint_advance_e": (_i32, [_vp, _f64, _f64, _f64, C.POINTER(CpicGrid), _f64, _i32, _vp]),
+    "cpic_adjoint_unload_accumulator": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64,
+                                               _i32, _vp]),
+    "cpic_adjoint_load_interpolator": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _i32, _vp]),
     "cpic_status_clear": (_i32, [_vp, _vp]),
     "cpic_status_read": (_i32, [_vp, _vp, C.POINTER(_i32)]),
 }

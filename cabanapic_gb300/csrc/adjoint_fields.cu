@@ -1,0 +1,227 @@
+// adjoint_fields.cu -- transposes of the linear per-cell maps of the step, for
+// the adjoint (reverse-mode) time step.  No counterpart in the reference.
+//
+// The field state is periodic: the reference's ghost copies (src/fields.h:
+// 11-100), its jf fold (src/fields.h:102-271) and its E update over [1, n+1]
+// (src/fields.h:646-664) keep every ghost value equal to the interior value at
+// its periodic image.  The forward maps are therefore periodic stencils on the
+// interior cells, and their adjoints are the transposed periodic stencils:
+//   advance_b   B' = B - Mb E        adjoint: lambda_E -= Mb^T lambda_B
+//   advance_e   E' = E - cj J + Me B adjoint: lambda_B += Me^T lambda_E, lambda_J = -cj lambda_E
+//   unload      J = U a              adjoint: lambda_a = U^T lambda_J
+//   interp      I = P (E, B)         adjoint: lambda_(E,B) += P^T lambda_I
+// Every transpose is written as a gather over the interior cells (no
+// atomics).  Adjoint arrays use the forward layouts: a field AoSoA holds
+// (lambda_E, lambda_B, lambda_J) in the (E, cB, jf) members; ghost cells are
+// unused.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace cpic {
+namespace {
+
+constexpr int kAdjThreads = 256;
+
+struct Periodic {
+  GridDev g;
+  __device__ int xp(int x) const { return x == g.nx ? 1 : x + 1; }
+  __device__ int xm(int x) const { return x == 1 ? g.nx : x - 1; }
+  __device__ int yp(int y) const { return y == g.ny ? 1 : y + 1; }
+  __device__ int ym(int y) const { return y == 1 ? g.ny : y - 1; }
+  __device__ int zp(int z) const { return z == g.nz ? 1 : z + 1; }
+  __device__ int zm(int z) const { return z == 1 ? g.nz : z - 1; }
+};
+
+__device__ __forceinline__ bool interior_coords(unsigned t, const GridDev& g, int& x, int& y, int& z) {
+  const unsigned ex = g.nx, ey = g.ny, ez = g.nz;
+  if (t >= ex * ey * ez) return false;
+  const unsigned r = t / ex;
+  x = (int)(t - r * ex) + 1;
+  z = (int)(r / ey);
+  y = (int)(r - (unsigned)z * ey) + 1;
+  z += 1;
+  return true;
+}
+
+template <class R>
+__device__ __forceinline__ R& fm(R* F, int c, int m) { return F[cell_at<9>(c, m)]; }
+
+// lambda_E -= Mb^T lambda_B, with Mb the forward-difference curl of advance_b
+// (src/fields.h:707-709) and coefficients (px, py, pz).
+template <class R>
+__global__ void __launch_bounds__(kAdjThreads)
+adj_advance_b_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz) {
+  int x, y, z;
+  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+  const Periodic P{g};
+  const int j = g.vox(x, y, z);
+  const int jxm = g.vox(P.xm(x), y, z), jym = g.vox(x, P.ym(y), z), jzm = g.vox(x, y, P.zm(z));
+  const R bx = fm(L, j, CPIC_F_CBX), by = fm(L, j, CPIC_F_CBY), bz = fm(L, j, CPIC_F_CBZ);
+  const R tex = pz * (fm(L, jzm, CPIC_F_CBY) - by) - py * (fm(L, jym, CPIC_F_CBZ) - bz);
+  const R tey = px * (fm(L, jxm, CPIC_F_CBZ) - bz) - pz * (fm(L, jzm, CPIC_F_CBX) - bx);
+  const R tez = py * (fm(L, jym, CPIC_F_CBX) - bx) - px * (fm(L, jxm, CPIC_F_CBY) - by);
+  fm(L, j, CPIC_F_EX) -= tex;
+  fm(L, j, CPIC_F_EY) -= tey;
+  fm(L, j, CPIC_F_EZ) -= tez;
+}
+
+// lambda_B += Me^T lambda_E and lambda_J = -cj lambda_E, with Me the
+// backward-difference curl of advance_e (src/fields.h:655-657).
+template <class R>
+__global__ void __launch_bounds__(kAdjThreads)
+adj_advance_e_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz, R cj) {
+  int x, y, z;
+  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+  const Periodic P{g};
+  const int j = g.vox(x, y, z);
+  const int jxp = g.vox(P.xp(x), y, z), jyp = g.vox(x, P.yp(y), z), jzp = g.vox(x, y, P.zp(z));
+  const R ex = fm(L, j, CPIC_F_EX), ey = fm(L, j, CPIC_F_EY), ez = fm(L, j, CPIC_F_EZ);
+  fm(L, j, CPIC_F_CBX) += pz * (ey - fm(L, jzp, CPIC_F_EY)) - py * (ez - fm(L, jyp, CPIC_F_EZ));
+  fm(L, j, CPIC_F_CBY) += px * (ez - fm(L, jxp, CPIC_F_EZ)) - pz * (ex - fm(L, jzp, CPIC_F_EX));
+  fm(L, j, CPIC_F_CBZ) += py * (ex - fm(L, jyp, CPIC_F_EX)) - px * (ey - fm(L, jxp, CPIC_F_EY));
+  fm(L, j, CPIC_F_JFX) = -cj * ex;
+  fm(L, j, CPIC_F_JFY) = -cj * ey;
+  fm(L, j, CPIC_F_JFZ) = -cj * ez;
+}
+
+// lambda_a = U^T lambda_J, U the periodic unload (src/accumulator.cpp:71-110
+// with the jf fold); writes the 12 adjoint accumulators of every interior cell.
+template <class R>
+__global__ void __launch_bounds__(kAdjThreads)
+adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R cx, R cy, R cz) {
+  int x, y, z;
+  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+  const Periodic P{g};
+  const int c = g.vox(x, y, z);
+  const int xp = P.xp(x), yp = P.yp(y), zp = P.zp(z);
+  auto lj = [&](int cc, int m) { return L[cell_at<9>(cc, m)]; };
+  R* a = A + (size_t)c * 12;
+  a[0] = cx * lj(c, CPIC_F_JFX);
+  a[1] = cx * lj(g.vox(x, yp, z), CPIC_F_JFX);
+  a[2] = cx * lj(g.vox(x, y, zp), CPIC_F_JFX);
+  a[3] = cx * lj(g.vox(x, yp, zp), CPIC_F_JFX);
+  a[4] = cy * lj(c, CPIC_F_JFY);
+  a[5] = cy * lj(g.vox(x, y, zp), CPIC_F_JFY);
+  a[6] = cy * lj(g.vox(xp, y, z), CPIC_F_JFY);
+  a[7] = cy * lj(g.vox(xp, y, zp), CPIC_F_JFY);
+  a[8] = cz * lj(c, CPIC_F_JFZ);
+  a[9] = cz * lj(g.vox(xp, y, z), CPIC_F_JFZ);
+  a[10] = cz * lj(g.vox(x, yp, z), CPIC_F_JFZ);
+  a[11] = cz * lj(g.vox(xp, yp, z), CPIC_F_JFZ);
+}
+
+// lambda_(E, B) += P^T lambda_I, P the interpolator load
+// (src/interpolator.cpp:80-131): each field value feeds the coefficients of up
+// to four cells (E) or two cells (B); gathered per field cell.
+template <class R>
+__global__ void __launch_bounds__(kAdjThreads)
+adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g) {
+  int x, y, z;
+  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+  const Periodic P{g};
+  const int j = g.vox(x, y, z);
+  const int xm = P.xm(x), ym = P.ym(y), zm = P.zm(z);
+  auto li = [&](int c, int m) { return LI[cell_at<18>(c, m)]; };
+  const R q = 0.25, h = 0.5;
+  // the four weights of a bilinear coefficient block (value, d/da, d/db, d2/dadb)
+  // for corners w0 (own), w1 (+a), w2 (+b), w3 (+a+b)
+  auto w0 = [&](int c, int m) { return q * (li(c, m) - li(c, m + 1) - li(c, m + 2) + li(c, m + 3)); };
+  auto w1 = [&](int c, int m) { return q * (li(c, m) + li(c, m + 1) - li(c, m + 2) - li(c, m + 3)); };
+  auto w2 = [&](int c, int m) { return q * (li(c, m) - li(c, m + 1) + li(c, m + 2) - li(c, m + 3)); };
+  auto w3 = [&](int c, int m) { return q * (li(c, m) + li(c, m + 1) + li(c, m + 2) + li(c, m + 3)); };
+  // ex: corners (i, i+y, i+z, i+y+z)
+  fm(L, j, CPIC_F_EX) += w0(j, CPIC_I_EX) + w1(g.vox(x, ym, z), CPIC_I_EX) +
+                         w2(g.vox(x, y, zm), CPIC_I_EX) + w3(g.vox(x, ym, zm), CPIC_I_EX);
+  // ey: corners (i, i+z, i+x, i+x+z)
+  fm(L, j, CPIC_F_EY) += w0(j, CPIC_I_EY) + w1(g.vox(x, y, zm), CPIC_I_EY) +
+                         w2(g.vox(xm, y, z), CPIC_I_EY) + w3(g.vox(xm, y, zm), CPIC_I_EY);
+  // ez: corners (i, i+x, i+y, i+x+y)
+  fm(L, j, CPIC_F_EZ) += w0(j, CPIC_I_EZ) + w1(g.vox(xm, y, z), CPIC_I_EZ) +
+                         w2(g.vox(x, ym, z), CPIC_I_EZ) + w3(g.vox(xm, ym, z), CPIC_I_EZ);
+  // cbx: (i, i+x); cby: (i, i+y); cbz: (i, i+z)
+  fm(L, j, CPIC_F_CBX) += h * (li(j, CPIC_I_CBX) - li(j, CPIC_I_DCBXDX)) +
+                          h * (li(g.vox(xm, y, z), CPIC_I_CBX) + li(g.vox(xm, y, z), CPIC_I_DCBXDX));
+  fm(L, j, CPIC_F_CBY) += h * (li(j, CPIC_I_CBY) - li(j, CPIC_I_DCBYDY)) +
+                          h * (li(g.vox(x, ym, z), CPIC_I_CBY) + li(g.vox(x, ym, z), CPIC_I_DCBYDY));
+  fm(L, j, CPIC_F_CBZ) += h * (li(j, CPIC_I_CBZ) - li(j, CPIC_I_DCBZDZ)) +
+                          h * (li(g.vox(x, y, zm), CPIC_I_CBZ) + li(g.vox(x, y, zm), CPIC_I_DCBZDZ));
+}
+
+inline unsigned nblocks(const GridDev& g) {
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  return (unsigned)((n + kAdjThreads - 1) / kAdjThreads);
+}
+
+}  // namespace
+}  // namespace cpic
+
+using namespace cpic;
+
+#define ADJ_PREAMBLE()                                                    \
+  int rc = check_grid(grid);                                              \
+  if (rc) return rc;                                                      \
+  if (precision != CPIC_FLOAT && precision != CPIC_DOUBLE) return CPIC_EINVAL; \
+  const GridDev g = make_grid(grid);                                      \
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream)
+
+extern "C" int cpic_adjoint_advance_b(void* d_lambda_fields, double px, double py, double pz,
+                                      const cpic_grid* grid, int32_t precision, cpic_stream_t stream) {
+  ADJ_PREAMBLE();
+  if (!d_lambda_fields) return CPIC_EINVAL;
+  if (precision == CPIC_FLOAT)
+    adj_advance_b_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<float*>(d_lambda_fields), g,
+                                                                   (float)px, (float)py, (float)pz);
+  else
+    adj_advance_b_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<double*>(d_lambda_fields), g,
+                                                                    px, py, pz);
+  return launch_status();
+}
+
+extern "C" int cpic_adjoint_advance_e(void* d_lambda_fields, double px, double py, double pz,
+                                      const cpic_grid* grid, double dt_eps0, int32_t precision,
+                                      cpic_stream_t stream) {
+  ADJ_PREAMBLE();
+  if (!d_lambda_fields) return CPIC_EINVAL;
+  if (precision == CPIC_FLOAT)
+    adj_advance_e_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<float*>(d_lambda_fields), g,
+                                                                   (float)px, (float)py, (float)pz,
+                                                                   (float)dt_eps0);
+  else
+    adj_advance_e_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<double*>(d_lambda_fields), g,
+                                                                    px, py, pz, dt_eps0);
+  return launch_status();
+}
+
+extern "C" int cpic_adjoint_unload_accumulator(const void* d_lambda_fields, void* d_lambda_acc,
+                                               const cpic_grid* grid, double dx, double dy, double dz,
+                                               double dt, int32_t precision, cpic_stream_t stream) {
+  ADJ_PREAMBLE();
+  if (!d_lambda_fields || !d_lambda_acc) return CPIC_EINVAL;
+  if (precision == CPIC_FLOAT) {
+    const float rdx = (float)dx, rdy = (float)dy, rdz = (float)dz, rdt = (float)dt;
+    adj_unload_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(
+        static_cast<const float*>(d_lambda_fields), static_cast<float*>(d_lambda_acc), g,
+        (float)(0.25 / (double)(float)(rdy * rdz * rdt)), (float)(0.25 / (double)(float)(rdz * rdx * rdt)),
+        (float)(0.25 / (double)(float)(rdx * rdy * rdt)));
+  } else {
+    adj_unload_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(
+        static_cast<const double*>(d_lambda_fields), static_cast<double*>(d_lambda_acc), g,
+        0.25 / (dy * dz * dt), 0.25 / (dz * dx * dt), 0.25 / (dx * dy * dt));
+  }
+  return launch_status();
+}
+
+extern "C" int cpic_adjoint_load_interpolator(const void* d_lambda_interp, void* d_lambda_fields,
+                                              const cpic_grid* grid, int32_t precision,
+                                              cpic_stream_t stream) {
+  ADJ_PREAMBLE();
+  if (!d_lambda_interp || !d_lambda_fields) return CPIC_EINVAL;
+  if (precision == CPIC_FLOAT)
+    adj_interp_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<const float*>(d_lambda_interp),
+                                                                static_cast<float*>(d_lambda_fields), g);
+  else
+    adj_interp_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<const double*>(d_lambda_interp),
+                                                                 static_cast<double*>(d_lambda_fields), g);
+  return launch_status();
+}

@@ -1,0 +1,338 @@
+// adjoint_push.cu -- reverse-mode (vector-Jacobian product) of push() for the
+// adjoint time step.  No counterpart in the reference.
+//
+// Forward map of one particle (src/push.h:66-295, src/move_p.h:93-371):
+//   (offsets x, momentum u, interpolator coefficients f[18] of its cell)
+//     -> (new offsets x', new momentum u', 12 current deposits per streak).
+// Given the adjoints of the outputs -- lambda_x', lambda_u' (the particle's
+// adjoint after the step) and lambda_a (the adjoint of the accumulator array,
+// read at the cells the particle deposits into: the transpose of the deposit
+// is a gather from the adjoint currents) -- the kernel recomputes the forward
+// push from the step's starting state and returns lambda_x, lambda_u (the
+// adjoint before the step, written in place) and adds lambda_f to the
+// adjoint interpolator array (the transpose of the gather, by atomics).
+//
+// Cell indices are piecewise constant: the streak split (which face is hit
+// first, how many streaks) is taken from the forward recompute, and the
+// derivative flows through the streak lengths and midpoints.  The particle
+// weight is not differentiated.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace cpic {
+namespace {
+
+constexpr int kAdjThreads = 128;
+constexpr int kMaxAdjStreaks = 8;  // a Courant-limited move needs at most 4
+
+template <class R>
+struct AdjArgs {
+  R qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp;
+  GridDev g;
+};
+
+template <class R>
+struct V3 {
+  R x, y, z;
+};
+template <class R>
+__device__ __forceinline__ V3<R> cross(V3<R> a, V3<R> b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class R>
+__device__ __forceinline__ R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+template <class R, bool LITERAL>
+__device__ __forceinline__ R root(R a) {
+  if constexpr (sizeof(R) == 8 && LITERAL) return (R)sqrtf((float)a);
+  else if constexpr (sizeof(R) == 8) return sqrt(a);
+  else return sqrtf(a);
+}
+
+// Adjoint of the 12 deposits of one streak: currents of charge q, streak s,
+// midpoint m (src/push.h:218-254, src/move_p.h:156-190), given their adjoints
+// la[12]; accumulates into ls, lm.
+template <class R>
+__device__ __forceinline__ void deposit_adjoint(R q, V3<R> s, V3<R> m, const R* la, V3<R>& ls, V3<R>& lm) {
+  const R one = 1;
+  R lcorr = 0;
+  auto block = [&](R qs, R da, R db, const R* A, R& lqs, R& lda, R& ldb) {
+    const R w0 = (one - da) * (one - db), w1 = (one + da) * (one - db);
+    const R w2 = (one - da) * (one + db), w3 = (one + da) * (one + db);
+    lqs = A[0] * w0 + A[1] * w1 + A[2] * w2 + A[3] * w3;
+    lda += qs * (-A[0] * (one - db) + A[1] * (one - db) - A[2] * (one + db) + A[3] * (one + db));
+    ldb += qs * (-A[0] * (one - da) - A[1] * (one + da) + A[2] * (one - da) + A[3] * (one + da));
+    lcorr += A[0] - A[1] - A[2] + A[3];
+  };
+  R lqx, lqy, lqz;
+  block(q * s.x, m.y, m.z, la + 0, lqx, lm.y, lm.z);  // jx: CALC_J(x,y,z)
+  block(q * s.y, m.z, m.x, la + 4, lqy, lm.z, lm.x);  // jy: CALC_J(y,z,x)
+  block(q * s.z, m.x, m.y, la + 8, lqz, lm.x, lm.y);  // jz: CALC_J(z,x,y)
+  const R third = R(1) / R(3);
+  ls.x += q * lqx + lcorr * q * s.y * s.z * third;
+  ls.y += q * lqy + lcorr * q * s.x * s.z * third;
+  ls.z += q * lqz + lcorr * q * s.x * s.y * third;
+}
+
+template <class R>
+__device__ __forceinline__ R comp(const V3<R>& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+template <class R>
+__device__ __forceinline__ void set_comp(V3<R>& v, int a, R val) {
+  if (a == 0) v.x = val; else if (a == 1) v.y = val; else v.z = val;
+}
+
+template <class R, int VL, bool LITERAL>
+__global__ void __launch_bounds__(kAdjThreads)
+adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
+                    const R* __restrict__ lacc, unsigned char* __restrict__ lpart, R* __restrict__ linterp,
+                    const AdjArgs<R> a, int* __restrict__ status) {
+  using L = PLayout<R, VL>;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  auto mem = [&](const unsigned char* b, int m) { return *reinterpret_cast<const R*>(b + L::off(p, m)); };
+  const V3<R> x0{mem(part, 0), mem(part, 1), mem(part, 2)};
+  const V3<R> u0{mem(part, 3), mem(part, 4), mem(part, 5)};
+  const R w = mem(part, 6);
+  const int cell = *reinterpret_cast<const int*>(part + L::cell_off(p));
+  const V3<R> lxo{mem(lpart, 0), mem(lpart, 1), mem(lpart, 2)};
+  const V3<R> luo{mem(lpart, 3), mem(lpart, 4), mem(lpart, 5)};
+  if ((unsigned)cell >= (unsigned)a.g.num_cells) {
+    atomicOr(status, CPIC_STATUS_CELL_RANGE);
+    return;
+  }
+  const R one = 1, k = a.qdt_2mc;
+  R f[18];
+#pragma unroll
+  for (int m = 0; m < 18; ++m) f[m] = __ldg(interp + cell_at<18>(cell, m));
+
+  // ---------------- forward recompute (push.h:124-182)
+  const V3<R> ha{k * ((f[0] + x0.y * f[1]) + x0.z * (f[2] + x0.y * f[3])),
+                 k * ((f[4] + x0.z * f[5]) + x0.x * (f[6] + x0.z * f[7])),
+                 k * ((f[8] + x0.x * f[9]) + x0.y * (f[10] + x0.x * f[11]))};
+  const V3<R> cb{f[12] + x0.x * f[13], f[14] + x0.y * f[15], f[16] + x0.z * f[17]};
+  const V3<R> u1{u0.x + ha.x, u0.y + ha.y, u0.z + ha.z};
+  const R g1 = one + dot(u1, u1);
+  const R b0 = k / root<R, LITERAL>(g1);
+  const R b1 = dot(cb, cb);
+  const R b2 = (b0 * b0) * b1;
+  const R P = one + b2 * (R(1. / 3.) + b2 * R(2. / 15.));
+  const R b3 = b0 * P;
+  const R D = one + b1 * (b3 * b3);
+  const R b4 = R(2) * b3 / D;
+  const V3<R> c1 = cross(u1, cb);
+  const V3<R> t{u1.x + b3 * c1.x, u1.y + b3 * c1.y, u1.z + b3 * c1.z};
+  const V3<R> c2 = cross(t, cb);
+  const V3<R> u3{u1.x + b4 * c2.x + ha.x, u1.y + b4 * c2.y + ha.y, u1.z + b4 * c2.z + ha.z};
+  const R g3 = one + dot(u3, u3);
+  const R rg = one / root<R, LITERAL>(g3);
+  const V3<R> cu{u3.x * a.cdt_dx, u3.y * a.cdt_dy, u3.z * a.cdt_dz};
+  const V3<R> d{cu.x * rg, cu.y * rg, cu.z * rg};
+  const R q = w * a.qsp;
+
+  // streak split (move_p.h:93-371; an in-cell move is one streak with axis 3)
+  V3<R> spos[kMaxAdjStreaks], srem[kMaxAdjStreaks];
+  R slen[kMaxAdjStreaks];
+  int saxis[kMaxAdjStreaks], scell[kMaxAdjStreaks];
+  int ns = 0;
+  {
+    V3<R> pos = x0, rem = d;
+    int c = cell;
+    const V3<R> np{x0.x + R(2) * d.x, x0.y + R(2) * d.y, x0.z + R(2) * d.z};
+    const bool inb = np.x <= one && np.y <= one && np.z <= one && -np.x <= one && -np.y <= one &&
+                     -np.z <= one;
+    bool done = false;
+    for (int it = 0; it < kMaxAdjStreaks; ++it) {
+      int axis = 3;
+      R len = 2;
+      if (!inb) {
+        for (int ax = 0; ax < 3; ++ax) {
+          const R r = comp(rem, ax);
+          const R dir = r > 0 ? R(1) : R(-1);
+          const R fr = (r == 0) ? R(3.4e38) : (dir - comp(pos, ax)) / r;
+          if (fr < len) { len = fr; axis = ax; }
+        }
+      }
+      len *= R(0.5);
+      spos[ns] = pos; srem[ns] = rem; slen[ns] = len; saxis[ns] = axis; scell[ns] = c;
+      ++ns;
+      const V3<R> s{rem.x * len, rem.y * len, rem.z * len};
+      // the face direction is the sign of the remaining displacement (move_p.h:109-111)
+      const R dir = axis < 3 && comp(rem, axis) > 0 ? R(1) : R(-1);
+      rem = {rem.x - s.x, rem.y - s.y, rem.z - s.z};
+      pos = {pos.x + s.x + s.x, pos.y + s.y + s.y, pos.z + s.z + s.z};
+      if (axis == 3) { done = true; break; }
+      int ix = c, iy, iz;
+      iy = ix / a.g.sx; ix -= iy * a.g.sx;
+      iz = iy / a.g.sy; iy -= iz * a.g.sy;
+      const int step = dir > 0 ? 1 : -1;
+      if (axis == 0) ix += step; else if (axis == 1) iy += step; else iz += step;
+      if (ix == 0) ix = a.g.nx; else if (ix == a.g.nx + 1) ix = 1;
+      if (iy == 0) iy = a.g.ny; else if (iy == a.g.ny + 1) iy = 1;
+      if (iz == 0) iz = a.g.nz; else if (iz == a.g.nz + 1) iz = 1;
+      c = a.g.vox(ix, iy, iz);
+      set_comp(pos, axis, -dir);
+    }
+    if (!done) {
+      atomicOr(status, CPIC_STATUS_MOVER_CAP);
+      return;
+    }
+  }
+
+  // ---------------- reverse: streaks (last to first)
+  V3<R> lpos = lxo, lrem{0, 0, 0};
+  for (int kk = ns - 1; kk >= 0; --kk) {
+    const int ax = saxis[kk];
+    const R len = slen[kk];
+    const V3<R> pos = spos[kk], rem = srem[kk];
+    const V3<R> s{rem.x * len, rem.y * len, rem.z * len};
+    const V3<R> mid{pos.x + s.x, pos.y + s.y, pos.z + s.z};
+    V3<R> ls{0, 0, 0}, lm{0, 0, 0}, lp{0, 0, 0};
+    // pos' = pos + 2 s, except the crossed axis, which is set to a constant
+    for (int b = 0; b < 3; ++b) {
+      if (b == ax) continue;
+      set_comp(lp, b, comp(lpos, b));
+      set_comp(ls, b, comp(ls, b) + R(2) * comp(lpos, b));
+    }
+    // rem' = rem - s
+    V3<R> lr = lrem;
+    ls = {ls.x - lrem.x, ls.y - lrem.y, ls.z - lrem.z};
+    // deposit of the streak into its cell
+    R la[12];
+    const R* ap = lacc + (size_t)scell[kk] * 12;
+#pragma unroll
+    for (int m = 0; m < 12; ++m) la[m] = __ldg(ap + m);
+    deposit_adjoint<R>(q, s, mid, la, ls, lm);
+    // mid = pos + s
+    lp = {lp.x + lm.x, lp.y + lm.y, lp.z + lm.z};
+    ls = {ls.x + lm.x, ls.y + lm.y, ls.z + lm.z};
+    // s = rem * len
+    lr = {lr.x + ls.x * len, lr.y + ls.y * len, lr.z + ls.z * len};
+    const R llen = dot(ls, rem);
+    if (ax < 3) {  // len = (dir - pos_ax) / (2 rem_ax)
+      const R r = comp(rem, ax);
+      set_comp(lp, ax, comp(lp, ax) - llen * R(0.5) / r);
+      set_comp(lr, ax, comp(lr, ax) - llen * len / r);
+    }
+    lpos = lp;
+    lrem = lr;
+  }
+  // lpos: adjoint of the starting offsets through the move; lrem: adjoint of d
+
+  // ---------------- reverse: displacement and Boris (push.h:144-182)
+  V3<R> lx = lpos;
+  V3<R> lu3{luo.x + lrem.x * a.cdt_dx * rg, luo.y + lrem.y * a.cdt_dy * rg, luo.z + lrem.z * a.cdt_dz * rg};
+  const R lrg = dot(lrem, cu);
+  const R lg3 = R(-0.5) * rg / g3 * lrg;
+  lu3 = {lu3.x + R(2) * u3.x * lg3, lu3.y + R(2) * u3.y * lg3, lu3.z + R(2) * u3.z * lg3};
+  V3<R> lha = lu3;  // u3 = u2 + ha
+  V3<R> lu1 = lu3;  // u2 = u1 + b4 (t x cb)
+  const R lb4 = dot(lu3, c2);
+  const V3<R> v{b4 * lu3.x, b4 * lu3.y, b4 * lu3.z};
+  V3<R> lt = cross(cb, v);
+  V3<R> lcb = cross(v, t);
+  // t = u1 + b3 (u1 x cb)
+  const V3<R> wv{b3 * lt.x, b3 * lt.y, b3 * lt.z};
+  const V3<R> cw = cross(cb, wv);
+  lu1 = {lu1.x + lt.x + cw.x, lu1.y + lt.y + cw.y, lu1.z + lt.z + cw.z};
+  R lb3 = dot(lt, c1);
+  const V3<R> wu = cross(wv, u1);
+  lcb = {lcb.x + wu.x, lcb.y + wu.y, lcb.z + wu.z};
+  // b4 = 2 b3 / D, D = 1 + b1 b3^2
+  lb3 += lb4 * R(2) * (one / D - R(2) * b1 * b3 * b3 / (D * D));
+  R lb1 = lb4 * (R(-2) * b3 * b3 * b3 / (D * D));
+  // b3 = b0 P(b2)
+  R lb0 = lb3 * P;
+  const R lb2 = lb3 * b0 * (R(1. / 3.) + R(4. / 15.) * b2);
+  // b2 = b0^2 b1
+  lb0 += lb2 * R(2) * b0 * b1;
+  lb1 += lb2 * b0 * b0;
+  // b1 = |cb|^2
+  lcb = {lcb.x + R(2) * cb.x * lb1, lcb.y + R(2) * cb.y * lb1, lcb.z + R(2) * cb.z * lb1};
+  // b0 = k / sqrt(g1)
+  const R lg1 = R(-0.5) * b0 / g1 * lb0;
+  lu1 = {lu1.x + R(2) * u1.x * lg1, lu1.y + R(2) * u1.y * lg1, lu1.z + R(2) * u1.z * lg1};
+  // u1 = u0 + ha
+  lha = {lha.x + lu1.x, lha.y + lu1.y, lha.z + lu1.z};
+
+  // ---------------- reverse: field at the particle (push.h:124-138)
+  R lf[18];
+  lf[0] = k * lha.x;
+  lf[1] = k * x0.y * lha.x;
+  lf[2] = k * x0.z * lha.x;
+  lf[3] = k * x0.y * x0.z * lha.x;
+  lx.y += k * (f[1] + x0.z * f[3]) * lha.x;
+  lx.z += k * (f[2] + x0.y * f[3]) * lha.x;
+  lf[4] = k * lha.y;
+  lf[5] = k * x0.z * lha.y;
+  lf[6] = k * x0.x * lha.y;
+  lf[7] = k * x0.x * x0.z * lha.y;
+  lx.z += k * (f[5] + x0.x * f[7]) * lha.y;
+  lx.x += k * (f[6] + x0.z * f[7]) * lha.y;
+  lf[8] = k * lha.z;
+  lf[9] = k * x0.x * lha.z;
+  lf[10] = k * x0.y * lha.z;
+  lf[11] = k * x0.x * x0.y * lha.z;
+  lx.x += k * (f[9] + x0.y * f[11]) * lha.z;
+  lx.y += k * (f[10] + x0.x * f[11]) * lha.z;
+  lf[12] = lcb.x; lf[13] = x0.x * lcb.x; lx.x += f[13] * lcb.x;
+  lf[14] = lcb.y; lf[15] = x0.y * lcb.y; lx.y += f[15] * lcb.y;
+  lf[16] = lcb.z; lf[17] = x0.z * lcb.z; lx.z += f[17] * lcb.z;
+
+  // adjoint before the step, in place
+  auto put = [&](int m, R v) { *reinterpret_cast<R*>(lpart + L::off(p, m)) = v; };
+  put(0, lx.x); put(1, lx.y); put(2, lx.z);
+  put(3, lu1.x); put(4, lu1.y); put(5, lu1.z);
+  // transpose of the gather
+  R* li = linterp;
+#pragma unroll
+  for (int m = 0; m < 18; ++m) red_add(li + cell_at<18>(cell, m), lf[m]);
+}
+
+template <class R, int VL, bool LITERAL>
+int launch_adjoint(const void* part, int n, const void* interp, const void* lacc, void* lpart, void* linterp,
+                   const AdjArgs<R>& a, int* status, cudaStream_t s) {
+  const unsigned blocks = (unsigned)(((int64_t)n + kAdjThreads - 1) / kAdjThreads);
+  adjoint_push_kernel<R, VL, LITERAL><<<blocks, kAdjThreads, 0, s>>>(
+      static_cast<const unsigned char*>(part), n, static_cast<const R*>(interp), static_cast<const R*>(lacc),
+      static_cast<unsigned char*>(lpart), static_cast<R*>(linterp), a, status);
+  return launch_status();
+}
+
+template <class R>
+int adjoint_typed(const void* part, int n, const void* interp, const void* lacc, void* lpart, void* linterp,
+                  const cpic_grid* g, const cpic_push_params* prm, int* status, cudaStream_t s) {
+  AdjArgs<R> a{(R)prm->qdt_2mc, (R)prm->cdt_dx, (R)prm->cdt_dy, (R)prm->cdt_dz, (R)prm->qsp, make_grid(g)};
+  const bool literal = !(prm->flags & CPIC_PUSH_TRUE_SQRT) && sizeof(R) == 8;
+  if (prm->particle_vl == 32)
+    return literal ? launch_adjoint<R, 32, true>(part, n, interp, lacc, lpart, linterp, a, status, s)
+                   : launch_adjoint<R, 32, false>(part, n, interp, lacc, lpart, linterp, a, status, s);
+  return literal ? launch_adjoint<R, 16, true>(part, n, interp, lacc, lpart, linterp, a, status, s)
+                 : launch_adjoint<R, 16, false>(part, n, interp, lacc, lpart, linterp, a, status, s);
+}
+
+}  // namespace
+}  // namespace cpic
+
+extern "C" int cpic_adjoint_push(const void* particles, int64_t num_particles, const void* interpolators,
+                                 const void* lambda_acc, void* lambda_particles, void* lambda_interp,
+                                 const cpic_grid* grid, const cpic_push_params* prm, int32_t* d_status,
+                                 cpic_stream_t stream) {
+  using namespace cpic;
+  if (!grid || !prm || !d_status) return CPIC_EINVAL;
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
+  if (prm->precision != CPIC_FLOAT && prm->precision != CPIC_DOUBLE) return CPIC_EINVAL;
+  if (prm->particle_vl != 16 && prm->particle_vl != 32) return CPIC_EINVAL;
+  if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT)) return CPIC_EINVAL;
+  if (num_particles == 0) return CPIC_OK;
+  if (!particles || !interpolators || !lambda_acc || !lambda_particles || !lambda_interp) return CPIC_EINVAL;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int n = (int)num_particles;
+  if (prm->precision == CPIC_FLOAT)
+    return adjoint_typed<float>(particles, n, interpolators, lambda_acc, lambda_particles, lambda_interp, grid,
+                                prm, d_status, s);
+  return adjoint_typed<double>(particles, n, interpolators, lambda_acc, lambda_particles, lambda_interp, grid,
+                               prm, d_status, s);
+}

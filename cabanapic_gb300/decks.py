@@ -194,7 +194,8 @@ def two_stream_1d_particles(deck: Deck) -> dict:
     cell = L.voxel(ix + 1, 1, 1, nx, 1)
     out = dict(x=off.astype(R), y=(rng.random(n) * 2 - 1).astype(R), z=(rng.random(n) * 2 - 1).astype(R),
                ux=ux.astype(R), uy=np.zeros(n, R), uz=np.zeros(n, R),
-               w=np.full(n, p["we"], R), cell=cell.astype(np.int32))
+               w=np.full(n, p["we"], R), cell=cell.astype(np.int32),
+               X=X, sign=sign)  # X, sign: the initial-condition parameters' inputs (not packed)
     order = np.argsort(out["cell"], kind="stable")
     return {k: v[order] for k, v in out.items()}
 

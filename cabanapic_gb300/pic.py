@@ -74,14 +74,17 @@ def _grid(nx, ny, nz, ng, boundary=Boundary.Periodic):
 # ---------------------------------------------------------------- push
 def push(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp,
          a0: AccumulatorArray, g, nx, ny, nz, num_ghosts, boundary, *, true_sqrt: bool = False,
-         stream=None) -> None:
+         exact: bool = False, stream=None) -> None:
     """push() (src/push.h:7-300): Boris push, move and current deposit.
 
-    `g` (grid_t*) is accepted and unused, as in the reference.  Adds into a0."""
+    `g` (grid_t*) is accepted and unused, as in the reference.  Adds into a0.
+    exact=True selects the bit-exact variant (unfused arithmetic, IEEE
+    division and sqrtf); the default uses fused multiply-adds and the hardware
+    reciprocal square root (within 1e-5 relative per particle)."""
     lib = capi.load()
+    flags = (capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0) | (capi.CPIC_PUSH_EXACT if exact else 0)
     prm = capi.CpicPushParams(float(qdt_2mc), float(cdt_dx), float(cdt_dy), float(cdt_dz),
-                              float(qsp), particles.precision, particles.vl,
-                              capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0, 0)
+                              float(qsp), particles.precision, particles.vl, flags, 0)
     if f0.precision != particles.precision or a0.precision != particles.precision:
         raise capi.CpicError("cpic_push", capi.CPIC_EINVAL, "mixed real_t precisions")
     grid = _grid(nx, ny, nz, num_ghosts, boundary)
@@ -218,3 +221,43 @@ class Sorter:
 
 def sort_particles(particles: ParticleList, num_cells: int, *, stream=None) -> None:
     Sorter(particles, num_cells)(particles, stream=stream)
+
+
+# ---------------------------------------------------------------- diagnostics
+class Diagnostics:
+    """FP64 charge density, Gauss residual (div E - rho/eps0) and kinetic
+    energy on the device (no counterpart in the reference)."""
+
+    def __init__(self, num_cells: int, device=None):
+        lib = capi.load()
+        dev = torch.device(device if device is not None else "cuda")
+        self.rho = torch.zeros(num_cells, dtype=torch.float64, device=dev)
+        self.scratch = torch.zeros(lib.raw("cpic_diag_scratch_bytes")(), dtype=torch.uint8, device=dev)
+        self.out = torch.zeros(4, dtype=torch.float64, device=dev)
+
+    def charge_density(self, particles: ParticleList, nx, ny, nz, ng, qsp, dx, dy, dz, *,
+                       boundary=Boundary.Periodic, stream=None) -> torch.Tensor:
+        capi.load().call("cpic_charge_density", particles.ptr, particles.n,
+                         C.byref(_grid(nx, ny, nz, ng, boundary)), particles.precision, particles.vl,
+                         float(qsp), float(dx), float(dy), float(dz), self.rho.data_ptr(),
+                         _STATUS.get().data_ptr(), _stream(stream))
+        return self.rho
+
+    def gauss_residual(self, fields: FieldArray, rho: torch.Tensor, nx, ny, nz, ng, dx, dy, dz,
+                       eps0=1.0, ref: torch.Tensor = None, resid: torch.Tensor = None, *,
+                       boundary=Boundary.Periodic, stream=None) -> torch.Tensor:
+        """Returns a device tensor {max|r|, sum r^2, sum (rho/eps0)^2}."""
+        out = torch.zeros(3, dtype=torch.float64, device=fields.buf.device)
+        capi.load().call("cpic_gauss_residual", fields.ptr, rho.data_ptr(),
+                         ref.data_ptr() if ref is not None else None, float(eps0), float(dx),
+                         float(dy), float(dz), C.byref(_grid(nx, ny, nz, ng, boundary)),
+                         fields.precision, resid.data_ptr() if resid is not None else None,
+                         out.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(), _stream(stream))
+        return out
+
+    def kinetic_energy(self, particles: ParticleList, mc2=1.0, *, stream=None) -> torch.Tensor:
+        out = torch.zeros(1, dtype=torch.float64, device=particles.buf.device)
+        capi.load().call("cpic_kinetic_energy", particles.ptr, particles.n, particles.precision,
+                         particles.vl, float(mc2), out.data_ptr(), self.scratch.data_ptr(),
+                         self.scratch.numel(), _stream(stream))
+        return out

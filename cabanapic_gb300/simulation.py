@@ -19,7 +19,7 @@ from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleLis
 
 class Simulation:
     def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
-                 max_steps: int = None, time_push: bool = False):
+                 max_steps: int = None, time_push: bool = False, exact: bool = False):
         self.deck = deck
         self.p = deck.derived()
         dev = torch.device(device if device is not None else "cuda")
@@ -42,6 +42,7 @@ class Simulation:
         self.step_no = 0
         self.time_push = time_push
         self.push_events = []
+        self.exact = bool(exact)
 
     # ------------------------------------------------------------------
     def step(self) -> None:
@@ -56,7 +57,7 @@ class Simulation:
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
         pic.push(self.particles, self.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
-                 p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary)
+                 p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary, exact=self.exact)
         if self.time_push:
             e1.record()
             self.push_events.append((e0, e1))

@@ -54,6 +54,11 @@ typedef struct CUstream_st* cpic_stream_t;
 /* cpic_push_params.flags */
 #define CPIC_PUSH_TRUE_SQRT 1  /* real_t=double only: use sqrt() for gamma where the
                                   reference calls sqrtf() (src/push.h:148,169) */
+#define CPIC_PUSH_EXACT 2      /* the exact variant: every multiply and add rounded
+                                  separately, IEEE division and sqrtf, so particle states
+                                  are bit-identical to a CPU build of the reference without
+                                  FMA contraction.  Default (0): fused multiply-adds and the
+                                  hardware reciprocal square root, within 1e-5 relative. */
 
 /* Grid of the run: interior cells nx*ny*nz plus num_ghosts ghost layers;
  * boundary is the deck's BOUNDARY_TYPE, which the reference's field code reads
@@ -168,6 +173,80 @@ size_t cpic_sort_scratch_bytes(int64_t num_particles, int64_t num_cells, int32_t
 int cpic_sort_particles(void* particles, int64_t num_particles, int64_t num_cells,
                         int32_t precision, int32_t particle_vl, void* d_scratch,
                         size_t scratch_bytes, cpic_stream_t stream);
+
+/* ---------------------------------------------------------------- diagnostics
+ * FP64 diagnostics with no counterpart in the reference (its only diagnostic
+ * is the field energy): what its scheme conserves, measured.
+ *
+ * cpic_charge_density overwrites d_rho (num_cells doubles, VOXEL-indexed
+ * nodes; node (i,j,k) is the low corner of voxel (i,j,k)) with the charge
+ * density of the particles: trilinear node weights (1 -/+ x)/2 (1 -/+ y)/2
+ * (1 -/+ z)/2 of the cell offsets, times qsp * w / (dx dy dz), with the
+ * periodic fold of the n+1 node layer into layer 1.  A particle whose cell
+ * is outside the grid is skipped and sets bit 1 of *d_status. */
+int cpic_charge_density(const void* particles, int64_t num_particles, const cpic_grid* grid,
+                        int32_t precision, int32_t particle_vl, double qsp, double dx, double dy,
+                        double dz, double* d_rho, int32_t* d_status, cpic_stream_t stream);
+
+/* Discrete Gauss residual r = div E - rho/eps0 (- d_ref, if not null) at the
+ * interior nodes, div E with backward differences of the edge fields
+ * ((ex(i) - ex(i-1))/dx + ...; periodic images for index 0).  The push's
+ * deposit and the Yee update keep r constant in time, so r(t) - r(0) measures
+ * charge-conservation error.  d_out = {max |r|, sum r^2, sum (rho/eps0)^2};
+ * d_resid (optional, num_cells doubles) receives r.  Deterministic. */
+size_t cpic_diag_scratch_bytes(void);
+int cpic_gauss_residual(const void* fields, const double* d_rho, const double* d_ref, double eps0,
+                        double dx, double dy, double dz, const cpic_grid* grid, int32_t precision,
+                        double* d_resid, double* d_out, void* d_scratch, size_t scratch_bytes,
+                        cpic_stream_t stream);
+
+/* Kinetic energy sum w * mc2 * (gamma - 1), gamma = sqrt(1 + u^2), in double
+ * (gamma - 1 computed as u^2 / (1 + gamma)), into d_out[0].  Deterministic. */
+int cpic_kinetic_energy(const void* particles, int64_t num_particles, int32_t precision,
+                        int32_t particle_vl, double mc2, double* d_out, void* d_scratch,
+                        size_t scratch_bytes, cpic_stream_t stream);
+
+/* ---------------------------------------------------------------- adjoint
+ * Reverse-mode (transposed) step kernels, no counterpart in the reference:
+ * gradients of a loss on the state after K steps with respect to the initial
+ * state.  Adjoint arrays use the forward layouts.  The field adjoints are the
+ * transposed periodic stencils (the reference's ghost copies and jf fold make
+ * the forward field maps periodic on the interior); ghost cells of adjoint
+ * arrays are unused.
+ *
+ * cpic_adjoint_push: given the particles at the START of the step, the
+ * step's interpolator, the adjoint accumulator array and, in
+ * lambda_particles, the adjoint of (offsets, momenta) after the step,
+ * overwrites lambda_particles with the adjoint before the step and adds the
+ * adjoint of the gathered coefficients into lambda_interp (transpose of the
+ * gather; the transpose of the deposit is a gather from lambda_acc).  Cell
+ * indices are piecewise constant; weights are not differentiated. */
+int cpic_adjoint_push(const void* particles, int64_t num_particles, const void* interpolators,
+                      const void* lambda_acc, void* lambda_particles, void* lambda_interp,
+                      const cpic_grid* grid, const cpic_push_params* prm, int32_t* d_status,
+                      cpic_stream_t stream);
+
+/* lambda_E -= Mb^T lambda_B: transpose of advance_b's cB update
+ * (src/fields.h:668-719), same (px, py, pz). */
+int cpic_adjoint_advance_b(void* d_lambda_fields, double px, double py, double pz,
+                           const cpic_grid* grid, int32_t precision, cpic_stream_t stream);
+
+/* lambda_B += Me^T lambda_E and lambda_J = -dt_eps0 lambda_E: transpose of
+ * advance_e (src/fields.h:618-665), lambda_J in the jf members. */
+int cpic_adjoint_advance_e(void* d_lambda_fields, double px, double py, double pz,
+                           const cpic_grid* grid, double dt_eps0, int32_t precision,
+                           cpic_stream_t stream);
+
+/* lambda_acc = unload^T lambda_J: transpose of unload_accumulator_array with
+ * its periodic fold (src/accumulator.cpp:45-122, src/fields.h:102-271). */
+int cpic_adjoint_unload_accumulator(const void* d_lambda_fields, void* d_lambda_acc,
+                                    const cpic_grid* grid, double dx, double dy, double dz,
+                                    double dt, int32_t precision, cpic_stream_t stream);
+
+/* lambda_(E, cB) += interp^T lambda_I: transpose of load_interpolator_array
+ * (src/interpolator.cpp:4-124). */
+int cpic_adjoint_load_interpolator(const void* d_lambda_interp, void* d_lambda_fields,
+                                   const cpic_grid* grid, int32_t precision, cpic_stream_t stream);
 
 /* ---------------------------------------------------------------- status */
 /* Clears the device status word (stream-ordered). */

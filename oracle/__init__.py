@@ -6,3 +6,4 @@ library (cabanapic_gb300) never imports it.
 """
 from .oracle import Oracle, load  # noqa: F401
 from . import energy_rule  # noqa: F401
+from . import diagnostics  # noqa: F401

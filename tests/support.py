@@ -92,3 +92,35 @@ def oracle_run(orc, deck, packed, steps):
 def history_deviation(a, b):
     """max_k |a_k - b_k| / max_k |b_k|, per column (E, B)."""
     return np.abs(a - b).max(axis=0) / np.abs(b).max(axis=0)
+
+
+def global_position(p, nx, ny, nz):
+    """Particle positions in half-cell units from the interior origin:
+    X = 2 (ix - 1) + (x + 1), and likewise for y and z."""
+    ix, iy, iz = L.rank_to_index(p["cell"].astype(np.int64), nx, ny)
+    return (2.0 * (ix - 1) + (p["x"].astype(np.float64) + 1),
+            2.0 * (iy - 1) + (p["y"].astype(np.float64) + 1),
+            2.0 * (iz - 1) + (p["z"].astype(np.float64) + 1))
+
+
+def assert_particles_close(got_bytes, ref_bytes, n, real, vl, nx, ny, nz, rtol=1e-5,
+                           max_cell_flips=1e-3):
+    """Per-particle tolerance check for the fused/approximate push: momenta to
+    rtol relative to |u|, positions to rtol of a cell width (periodic, in
+    global coordinates, so a particle that ends exactly on a face in one
+    result and just across it in the other still compares equal), weights
+    exact, and cell indices equal except for such face cases."""
+    g = L.unpack_particles(got_bytes, n, real, vl)
+    r = L.unpack_particles(ref_bytes, n, real, vl)
+    assert np.array_equal(g["w"], r["w"])
+    un = np.sqrt(sum(r[k].astype(np.float64) ** 2 for k in ("ux", "uy", "uz")))
+    for k in ("ux", "uy", "uz"):
+        d = np.abs(g[k].astype(np.float64) - r[k])
+        assert np.all(d <= rtol * un + 1e-30), (k, (d / np.maximum(un, 1e-30)).max())
+    for a, b, m in zip(global_position(g, nx, ny, nz), global_position(r, nx, ny, nz), (nx, ny, nz)):
+        d = a - b
+        d = (d + m) % (2 * m) - m  # periodic
+        assert np.all(np.abs(d) <= 2 * rtol), np.abs(d).max()
+    flips = np.count_nonzero(g["cell"] != r["cell"])
+    assert flips <= max(1, max_cell_flips * n), flips
+    return flips

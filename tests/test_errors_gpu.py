@@ -53,7 +53,8 @@ def test_nonfinite_momentum_is_reported(orc):
     host["ux"][17] = np.nan
     st["particles"] = L.pack_particles(host, np.float32, 32)
     P, I, A = _setup(st)
-    pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic)
+    pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic,
+             exact=True)
     with pytest.raises(capi.CpicDeviceError) as ei:
         pic.check_status()
     assert ei.value.bits & capi.CPIC_STATUS_NONFINITE

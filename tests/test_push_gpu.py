@@ -1,22 +1,26 @@
 """Parity of the GPU push (cpic_push through the C ABI) against the oracle.
 
-Particle state (offsets, momenta, cell index) must be bit-identical: the
-kernel and the oracle perform the reference's arithmetic in the same order
-with separately rounded operations.  Accumulators are sums of the same terms
-in a different order (warp reductions and atomics), so they must agree within
-the recursive-summation bound 2 (k-1) eps sum|x| per accumulator.
+Exact variant (CPIC_PUSH_EXACT): particle state (offsets, momenta, cell
+index) must be bit-identical, because the kernel and the oracle perform the
+reference's arithmetic in the same order with separately rounded operations.
+Default variant (fused multiply-adds, hardware reciprocal square root): every
+particle within 1e-5 relative (the FP32 tolerance stated for this path), cell
+indices equal except where a particle ends on a face.  Accumulators are sums
+of the same terms in a different order (warp reductions and atomics), so they
+must agree within the recursive-summation bound 2 (k-1) eps sum|x| per
+accumulator (plus 1e-5 sum|x| for the default variant's per-term rounding).
 """
 import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
 
-from support import random_state, reorder_bound  # noqa: E402
+from support import assert_particles_close, random_state, reorder_bound  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
 
-def _run_pair(orc, st, true_sqrt=False):
+def _run_pair(orc, st, true_sqrt=False, exact=True):
     from cabanapic_gb300 import pic
     R = st["real"]
     nc = st["num_cells"]
@@ -31,18 +35,27 @@ def _run_pair(orc, st, true_sqrt=False):
     I.buf.copy_(torch.from_numpy(st["interp"]))
     A = pic.AccumulatorArray(nc, R)
     pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic,
-             true_sqrt=true_sqrt)
+             true_sqrt=true_sqrt, exact=exact)
     pic.check_status()
     return host, acc, acc_abs, cnt, P.download_bytes(), A.get(), crossers
 
 
-def _assert_parity(res, real):
+def _assert_parity(res, real, st=None, exact=True):
     host, acc, acc_abs, cnt, gpu_p, gpu_acc, _ = res
-    assert np.array_equal(gpu_p, host), "particle AoSoA bytes differ from the oracle"
     eps = np.finfo(real).eps
     bound = reorder_bound(acc_abs, cnt, eps)
+    if exact:
+        assert np.array_equal(gpu_p, host), "particle AoSoA bytes differ from the oracle"
+    else:
+        assert_particles_close(gpu_p, host, st["n"], real, st["vl"], st["nx"], st["ny"], st["nz"])
+        bound = bound + 1e-5 * acc_abs + 1e-6 * float(acc_abs.max())
     err = np.abs(gpu_acc.astype(np.float64) - acc.astype(np.float64))
-    assert np.all(err <= bound), f"accumulator error {err.max():.3e} above the reordering bound"
+    assert np.all(err <= bound), f"accumulator error {err.max():.3e} above the bound"
+
+
+def _both(orc, st, real, **kw):
+    _assert_parity(_run_pair(orc, st, exact=True, **kw), real, st, exact=True)
+    _assert_parity(_run_pair(orc, st, exact=False, **kw), real, st, exact=False)
 
 
 @pytest.mark.parametrize("sort", [False, True])
@@ -51,31 +64,32 @@ def test_push_float_vl32(orc, sort, n):
     st = random_state(nx=6, ny=5, nz=4, n=n, seed=n + int(sort), sort=sort)
     res = _run_pair(orc, st)
     _assert_parity(res, np.float32)
+    _assert_parity(_run_pair(orc, st, exact=False), np.float32, st, exact=False)
     if n >= 4000:
         assert res[-1] > 0.2 * n  # the crossing path was exercised
 
 
 def test_push_float_vl16(orc):
     st = random_state(nx=5, ny=4, nz=6, n=9999, seed=3, vl=16)
-    _assert_parity(_run_pair(orc, st), np.float32)
+    _both(orc, st, np.float32)
 
 
 @pytest.mark.parametrize("true_sqrt", [False, True])
 def test_push_double(orc, true_sqrt):
     st = random_state(nx=4, ny=6, nz=5, n=6007, seed=11, real=np.float64)
-    _assert_parity(_run_pair(orc, st, true_sqrt=true_sqrt), np.float64)
+    _both(orc, st, np.float64, true_sqrt=true_sqrt)
 
 
 def test_push_collapsed_axes(orc):
     # a 1-D grid (ny = nz = 1), like the reference's 2stream decks
     st = random_state(nx=32, ny=1, nz=1, n=5000, seed=5, cdt=(0.5, 0.2, 0.2))
-    _assert_parity(_run_pair(orc, st), np.float32)
+    _both(orc, st, np.float32)
 
 
 def test_push_dense_cells_sorted(orc):
     # 64+ particles per cell in cell order: the warp-reduction path dominates
     st = random_state(nx=4, ny=4, nz=4, n=64 * 64 + 17, seed=9, sort=True, crossing=0.05)
-    _assert_parity(_run_pair(orc, st), np.float32)
+    _both(orc, st, np.float32)
 
 
 def test_push_accumulates_into_existing_values(orc):
@@ -92,6 +106,34 @@ def test_push_accumulates_into_existing_values(orc):
     I.buf.copy_(torch.from_numpy(st["interp"]))
     A = pic.AccumulatorArray(nc, np.float32)
     A.set(start)
-    pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic)
+    pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic,
+             exact=True)
     pic.check_status()
     assert np.allclose(A.get(), acc, rtol=1e-5, atol=1e-5)
+
+
+def test_fast_and_exact_agree_on_a_thermal_plasma(orc):
+    """Both variants on the benchmark's kind of input (sorted thermal plasma)."""
+    from cabanapic_gb300 import decks, layout as L, pic
+    deck = decks.thermal(n=12, ppc=32, num_steps=1, seed=5)
+    p = deck.derived()
+    host = L.pack_particles(decks.thermal_particles(deck), np.float32, 32)
+    nc = deck.num_cells
+    rng = np.random.default_rng(1)
+    interp = L.pack_cells((rng.standard_normal((nc, 18)) * 0.05).astype(np.float32), np.float32)
+    out = {}
+    for exact in (True, False):
+        P = pic.ParticleList(deck.num_particles, np.float32, 32).upload(host)
+        I = pic.InterpolatorArray(nc, np.float32)
+        I.buf.copy_(torch.from_numpy(interp))
+        A = pic.AccumulatorArray(nc, np.float32)
+        pic.push(P, I, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"], p["qsp"], A, None,
+                 12, 12, 12, 1, pic.Boundary.Periodic, exact=exact)
+        pic.check_status()
+        out[exact] = (P.download_bytes(), A.get())
+    ref = host.copy()
+    acc = np.zeros((nc, 3, 4), np.float32)
+    orc.push(ref, deck.num_particles, 32, interp, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"],
+             p["cdt_dz"], p["qsp"], acc, orc.grid(12, 12, 12))
+    assert np.array_equal(out[True][0], ref)
+    assert_particles_close(out[False][0], ref, deck.num_particles, np.float32, 32, 12, 12, 12)

@@ -50,7 +50,7 @@ def test_sort_then_push_matches_oracle(orc):
     I = pic.InterpolatorArray(nc, np.float32)
     I.buf.copy_(torch.from_numpy(st["interp"]))
     A = pic.AccumulatorArray(nc, np.float32)
-    pic.push(P, I, *st["push_args"], A, None, 8, 8, 8, 1, pic.Boundary.Periodic)
+    pic.push(P, I, *st["push_args"], A, None, 8, 8, 8, 1, pic.Boundary.Periodic, exact=True)
     pic.check_status()
     assert np.array_equal(P.download_bytes(), host)
     err = np.abs(A.get().astype(np.float64) - acc)
