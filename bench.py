@@ -119,14 +119,28 @@ def _dist():
     return ws, rank, local
 
 
-def _barrier_max(x, ws):
+def _barrier_max(x, ws, device="cuda"):
+    """Max of a per-rank time over the ranks (the slowest replica sets the time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(units_per_rank, ms_per_rank, ws, device="cuda"):
+    """Whole-job throughput of N independent replicas: all ranks' units over
+    the slowest rank's time (units/s)."""
+    if ws == 1:
+        return units_per_rank / (ms_per_rank / 1e3), ms_per_rank
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(units_per_rank)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    ms = _barrier_max(ms_per_rank, ws, device)
+    return float(t.item()) / (ms / 1e3), ms
 
 
 def _barrier(ws):
@@ -311,8 +325,7 @@ def main():
     clocks = sampler.stop()
     deck = res["deck"]
     n = deck.num_particles
-    ms = _barrier_max(res["ms"], ws)
-    value = n * args.steps * ws / (ms / 1e3)
+    value, ms = replica_throughput(n * args.steps, res["ms"], ws)
     push_ms = float(np.mean(res["push_ms"]))
     alg_bytes = n * BYTES_PER_PARTICLE[4] + deck.num_interior * BYTES_PER_CELL[4]
     peak, peak_kind = _peaks()

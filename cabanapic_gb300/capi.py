@@ -98,6 +98,9 @@ _SIGS = {
     "cpic_adjoint_unload_accumulator": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64,
                                                _i32, _vp]),
     "cpic_adjoint_load_interpolator": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _i32, _vp]),
+    "cpic_uncenter_particles": (_i32, [_vp, _i64, _vp, _f64, C.POINTER(CpicGrid), _i32, _i32, _vp, _vp]),
+    "cpic_es_advance_e": (_i32, [_vp, C.POINTER(CpicGrid), _f64, _i32, _i32, _vp]),
+    "cpic_es_e_energy": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _vp, _vp, _sz, _vp]),
     "cpic_status_clear": (_i32, [_vp, _vp]),
     "cpic_status_read": (_i32, [_vp, _vp, C.POINTER(_i32)]),
 }

@@ -257,6 +257,54 @@ energy_kernel(const R* __restrict__ F, const GridDev g, double* __restrict__ out
   }
 }
 
+// ------------------------------------------------------------ ES solver
+// ES_Field_Solver(_1D)::advance_e (fields.h:400-436, 511-544): E -= cj J over
+// every cell of the array (ghosts included, as the reference does); the 1-D
+// variant folds the jf ghosts first (same fold as the EM path).
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+es_advance_e_kernel(R* __restrict__ F, int num_cells, R cj) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= num_cells) return;
+  F[cell_at<9>(i, CPIC_F_EX)] = F[cell_at<9>(i, CPIC_F_EX)] + (-cj * F[cell_at<9>(i, CPIC_F_JFX)]);
+  F[cell_at<9>(i, CPIC_F_EY)] = F[cell_at<9>(i, CPIC_F_EY)] + (-cj * F[cell_at<9>(i, CPIC_F_JFY)]);
+  F[cell_at<9>(i, CPIC_F_EZ)] = F[cell_at<9>(i, CPIC_F_EZ)] + (-cj * F[cell_at<9>(i, CPIC_F_JFZ)]);
+}
+
+// ES e_energy (fields.h:438-463, 484-509): 0.5 sum over every cell of E^2, in
+// double with the fixed-tree reduction of the EM energies (out[1] = 0).
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+es_energy_kernel(const R* __restrict__ F, int num_cells, double* __restrict__ out,
+                 EnergyScratch* __restrict__ sc) {
+  __shared__ double se[kThreads / 32];
+  __shared__ bool last;
+  double e = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num_cells; i += gridDim.x * blockDim.x) {
+    const double a0 = F[cell_at<9>(i, CPIC_F_EX)], a1 = F[cell_at<9>(i, CPIC_F_EY)], a2 = F[cell_at<9>(i, CPIC_F_EZ)];
+    e += a0 * a0 + a1 * a1 + a2 * a2;
+  }
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
+  if ((threadIdx.x & 31) == 0) se[threadIdx.x >> 5] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < kThreads / 32; ++k) t += se[k];
+    sc->part[2 * blockIdx.x] = t;
+    __threadfence();
+    last = (atomicAdd(&sc->done, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double t = 0.0;
+    for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(&sc->part[2 * k]);
+    out[0] = t * 0.5;
+    out[1] = 0.0;
+    sc->done = 0;
+  }
+}
+
 // ------------------------------------------------------------ host side
 template <class R>
 static int typed_load_interp(const void* f, void* i, const GridDev& g, cudaStream_t s) {
@@ -479,6 +527,47 @@ extern "C" int cpic_field_energies_noalloc(const void* fields, const cpic_grid* 
   const GridDev g = make_grid(grid);
   return precision == CPIC_FLOAT ? typed_energies<float>(fields, g, d_out, sc, s)
                                  : typed_energies<double>(fields, g, d_out, sc, s);
+}
+
+extern "C" int cpic_es_advance_e(void* fields, const cpic_grid* grid, double dt_eps0, int32_t fold_ghosts,
+                                 int32_t precision, cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields) return CPIC_EINVAL;
+  const GridDev g = make_grid(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int outer = g.nx > g.ny ? g.nx : g.ny;
+  outer = outer > g.nz ? outer : g.nz;
+  if (precision == CPIC_FLOAT) {
+    if (fold_ghosts) current_fold_kernel<float><<<dim3((unsigned)outer, 3), 128, 0, s>>>(static_cast<float*>(fields), g);
+    es_advance_e_kernel<float><<<blocks_for(g.num_cells), kThreads, 0, s>>>(static_cast<float*>(fields), g.num_cells,
+                                                                           (float)dt_eps0);
+  } else {
+    if (fold_ghosts) current_fold_kernel<double><<<dim3((unsigned)outer, 3), 128, 0, s>>>(static_cast<double*>(fields), g);
+    es_advance_e_kernel<double><<<blocks_for(g.num_cells), kThreads, 0, s>>>(static_cast<double*>(fields), g.num_cells,
+                                                                            dt_eps0);
+  }
+  return launch_status();
+}
+
+extern "C" int cpic_es_e_energy(const void* fields, const cpic_grid* grid, int32_t precision, double* d_out,
+                                void* d_scratch, size_t scratch_bytes, cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields || !d_out || !d_scratch) return CPIC_EINVAL;
+  if (scratch_bytes < sizeof(EnergyScratch)) return CPIC_ESCRATCH;
+  if (((uintptr_t)d_scratch & 7) || ((uintptr_t)d_out & 7)) return CPIC_EINVAL;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  EnergyScratch* sc = static_cast<EnergyScratch*>(d_scratch);
+  if (cudaMemsetAsync(&sc->done, 0, sizeof(unsigned), s) != cudaSuccess) return CPIC_ECUDA;
+  const GridDev g = make_grid(grid);
+  if (precision == CPIC_FLOAT)
+    es_energy_kernel<float><<<kEnergyBlocks, kThreads, 0, s>>>(static_cast<const float*>(fields), g.num_cells, d_out, sc);
+  else
+    es_energy_kernel<double><<<kEnergyBlocks, kThreads, 0, s>>>(static_cast<const double*>(fields), g.num_cells, d_out, sc);
+  return launch_status();
 }
 
 extern "C" int cpic_status_clear(int32_t* d_status, cpic_stream_t stream) {

@@ -26,8 +26,9 @@
 //     through the read-only cache; after a cell sort a warp mostly shares one
 //     cell, so the gather is a broadcast;
 //   * in-cell particles deposit their 12 currents through a warp reduction:
-//     when the whole warp is in one cell, a 13-shuffle reduce-scatter leaves
-//     one total per lane and 12 lanes write it with one atomic each;
+//     when every depositing lane of the warp is in one cell, a 13-shuffle
+//     reduce-scatter leaves one total per lane and 12 lanes write it with one
+//     atomic each;
 //     otherwise the largest group of lanes sharing a cell is reduced that way
 //     and the other lanes use 16-byte vector reductions (red.global.add.v4);
 //   * cell-crossing particles are compacted into a per-warp shared-memory
@@ -156,9 +157,14 @@ __device__ __forceinline__ int value_of_lane(int lane) {
 template <class R>
 __device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool dep,
                                              const R v[12], int lane, int vi) {
-  const int cell0 = __shfl_sync(kFull, cell, 0);
-  if (__all_sync(kFull, dep && cell == cell0)) {  // one cell for the whole warp
-    const R tot = reduce_scatter12<R>(v, lane);
+  const unsigned dm = __ballot_sync(kFull, dep);
+  if (dm == 0u) return;
+  const int cell0 = __shfl_sync(kFull, cell, __ffs(dm) - 1);
+  if (__all_sync(kFull, !dep || cell == cell0)) {  // every depositing lane in one cell
+    R w[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) w[k] = dep ? v[k] : R(0);
+    const R tot = reduce_scatter12<R>(w, lane);
     if (vi >= 0) red_add(acc + (size_t)cell0 * 12 + vi, tot);
     return;
   }

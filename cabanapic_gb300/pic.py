@@ -98,6 +98,17 @@ def grid_cells(nx, ny, nz, ng=1) -> int:
     return (nx + 2 * ng) * (ny + 2 * ng) * (nz + 2 * ng)
 
 
+def uncenter_particles(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, *, nx, ny, nz,
+                       num_ghosts=1, stream=None) -> None:
+    """uncenter_particles (src/uncenter_p.h:4-105): t = 0 back half-step of u.
+
+    The grid extents are keyword arguments (the reference reads none; they
+    bound-check the cell indices here)."""
+    capi.load().call("cpic_uncenter_particles", particles.ptr, particles.n, f0.ptr, float(qdt_2mc),
+                     C.byref(_grid(nx, ny, nz, num_ghosts)), particles.precision, particles.vl,
+                     _STATUS.get().data_ptr(), _stream(stream))
+
+
 # ---------------------------------------------------------------- cells
 def load_interpolator_array(fields: FieldArray, interpolators: InterpolatorArray, nx, ny, nz, ng,
                             *, boundary=Boundary.Periodic, stream=None) -> None:
@@ -175,6 +186,38 @@ class EMFieldSolver:
     def b_energy(self, fields: FieldArray, px, py, pz, nx, ny, nz, ng, *, stream=None) -> float:
         """EM_Field_Solver::b_energy (fields.h:588-615), accumulated in double."""
         return float(self.energies_async(fields, nx, ny, nz, ng, stream=stream)[1].item())
+
+
+class ESFieldSolver1D:
+    """Field_Solver<ES_Field_Solver_1D> (src/fields.h:467-545): advance_b is a
+    no-op; advance_e folds the jf ghosts and applies E -= dt_eps0 J on every
+    cell; e_energy sums E^2 over every cell (ghosts included), in double.
+    one_d=False gives ES_Field_Solver (src/fields.h:382-464, no fold)."""
+
+    def __init__(self, fields: FieldArray = None, boundary=Boundary.Periodic, one_d: bool = True):
+        self.boundary = Boundary(boundary)
+        self.one_d = bool(one_d)
+        self._scratch = None
+        if fields is not None:
+            fields.buf.zero_()
+
+    def advance_b(self, fields, px, py, pz, nx, ny, nz, ng, *, stream=None) -> None:
+        return None
+
+    def advance_e(self, fields: FieldArray, px, py, pz, nx, ny, nz, ng, dt_eps0, *, stream=None) -> None:
+        capi.load().call("cpic_es_advance_e", fields.ptr, C.byref(_grid(nx, ny, nz, ng, self.boundary)),
+                         float(dt_eps0), int(self.one_d), fields.precision, _stream(stream))
+
+    def e_energy(self, fields: FieldArray, px, py, pz, nx, ny, nz, ng, *, stream=None) -> float:
+        lib = capi.load()
+        if self._scratch is None:
+            self._scratch = torch.zeros(lib.raw("cpic_energy_scratch_bytes")(), dtype=torch.uint8,
+                                        device=fields.buf.device)
+        out = torch.zeros(2, dtype=torch.float64, device=fields.buf.device)
+        lib.call("cpic_es_e_energy", fields.ptr, C.byref(_grid(nx, ny, nz, ng, self.boundary)),
+                 fields.precision, out.data_ptr(), self._scratch.data_ptr(), self._scratch.numel(),
+                 _stream(stream))
+        return float(out[0].item())
 
 
 def dump_energies(field_solver: EMFieldSolver, fields: FieldArray, step, time, px, py, pz, nx, ny,

@@ -162,6 +162,30 @@ int cpic_field_energies(const void* fields, const cpic_grid* grid, int32_t preci
 int cpic_field_energies_noalloc(const void* fields, const cpic_grid* grid, int32_t precision,
                                 double* d_out, cpic_stream_t stream);
 
+/* Replaces: void uncenter_particles(particle_list_t particles,
+ *   interpolator_array_t& f0, real_t qdt_2mc)          -- src/uncenter_p.h:4-105
+ * The optional t = 0 back half-step of the momenta (example/example.cpp:204-213):
+ * Boris rotation with -qdt_2mc/2, then the half E kick, in place.  `grid` is
+ * used to check the particles' cell indices; a bad one sets
+ * CPIC_STATUS_CELL_RANGE and leaves the particle unchanged. */
+int cpic_uncenter_particles(void* particles, int64_t num_particles, const void* interpolators,
+                            double qdt_2mc, const cpic_grid* grid, int32_t precision,
+                            int32_t particle_vl, int32_t* d_status, cpic_stream_t stream);
+
+/* Replaces: ES_Field_Solver_1D::advance_e (src/fields.h:511-544) with
+ * fold_ghosts = 1 (the periodic jf fold, then E -= dt_eps0 * J) and
+ * ES_Field_Solver::advance_e (src/fields.h:400-436) with fold_ghosts = 0; the
+ * E update covers every cell of the array, ghosts included, as in the
+ * reference.  (The ES solvers' advance_b is a no-op.) */
+int cpic_es_advance_e(void* fields, const cpic_grid* grid, double dt_eps0, int32_t fold_ghosts,
+                      int32_t precision, cpic_stream_t stream);
+
+/* Replaces: ES e_energy (src/fields.h:438-463, 484-509): d_out[0] = 0.5 * sum
+ * over every cell (ghosts included, as in the reference) of E^2, in double;
+ * d_out[1] = 0.  Scratch as cpic_field_energies. */
+int cpic_es_e_energy(const void* fields, const cpic_grid* grid, int32_t precision, double* d_out,
+                     void* d_scratch, size_t scratch_bytes, cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- sort
  * Counting sort of the particle list by cell index, in place.  The reference
  * leaves this step commented out (example/example.cpp:226-228, Cabana::sortByKey);

@@ -318,6 +318,44 @@ void push_openmp(const Particles<R>& P, size_t n, const R* interp, R qdt_2mc, R 
   }
 }
 
+// ---------------------------------------------------------------- uncenter
+// uncenter_particles, src/uncenter_p.h:4-105: Boris rotation with
+// qdt_4mc = -0.5*qdt_2mc, then the half E kick (in that order, as written).
+template <class R>
+void uncenter(const Particles<R>& P, size_t n, const R* interp, R qdt_2mc) {
+  CellSoA<R, kInterpMembers> f{const_cast<R*>(interp)};
+  const R qdt_4mc = -0.5 * qdt_2mc;
+  const R one = 1.;
+  const R one_third = 1. / 3.;
+  const R two_fifteenths = 2. / 15.;
+  for (size_t p = 0; p < n; ++p) {
+    R dx = P.mem(0, p), dy = P.mem(1, p), dz = P.mem(2, p);
+    long ii = P.cell(p);
+    R hax = qdt_2mc * ((f(ii, EX) + dy * f(ii, DEXDY)) + dz * (f(ii, DEXDZ) + dy * f(ii, D2EXDYDZ)));
+    R hay = qdt_2mc * ((f(ii, EY) + dz * f(ii, DEYDZ)) + dx * (f(ii, DEYDX) + dz * f(ii, D2EYDZDX)));
+    R haz = qdt_2mc * ((f(ii, EZ) + dx * f(ii, DEZDX)) + dy * (f(ii, DEZDY) + dx * f(ii, D2EZDXDY)));
+    R cbx = f(ii, CBX) + dx * f(ii, DCBXDX);
+    R cby = f(ii, CBY) + dy * f(ii, DCBYDY);
+    R cbz = f(ii, CBZ) + dz * f(ii, DCBZDZ);
+    R ux = P.mem(3, p), uy = P.mem(4, p), uz = P.mem(5, p);
+    // (real_t)sqrt(real_t): exact as sqrtf for float
+    R v0 = qdt_4mc / (R)std::sqrt(one + (ux * ux + (uy * uy + uz * uz)));
+    R v1 = cbx * cbx + (cby * cby + cbz * cbz);
+    R v2 = (v0 * v0) * v1;
+    R v3 = v0 * (one + v2 * (one_third + v2 * two_fifteenths));
+    R v4 = v3 / (one + v1 * (v3 * v3));
+    v4 += v4;
+    R t0 = ux + v3 * (uy * cbz - uz * cby);
+    R t1 = uy + v3 * (uz * cbx - ux * cbz);
+    R t2 = uz + v3 * (ux * cby - uy * cbx);
+    ux += v4 * (t1 * cbz - t2 * cby);
+    uy += v4 * (t2 * cbx - t0 * cbz);
+    uz += v4 * (t0 * cby - t1 * cbx);
+    ux += hax; uy += hay; uz += haz;
+    P.mem(3, p) = ux; P.mem(4, p) = uy; P.mem(5, p) = uz;
+  }
+}
+
 // ---------------------------------------------------------------- interpolator
 // load_interpolator_array, src/interpolator.cpp:4-124, interior cells only.
 template <class R>
@@ -452,6 +490,31 @@ void advance_e(R* fields, R px, R py, R pz, const Grid& g, R dt_eps0) {
         F(f0, F_EZ) = F(f0, F_EZ) + (-cj * F(f0, F_JFZ)) +
                       (px * (F(f0, F_CBY) - F(fx, F_CBY)) - py * (F(f0, F_CBX) - F(fy, F_CBX)));
       }
+}
+
+// ES solvers, src/fields.h:382-545: (1-D: jf fold first) E -= cj J over every
+// cell of the array; e_energy over every cell (ghosts included), double sum.
+template <class R>
+void es_advance_e(R* fields, const Grid& g, R dt_eps0, bool fold) {
+  CellSoA<R, kFieldMembers> F{fields};
+  if (fold) current_fold<R>(fields, g);
+  const R cj = dt_eps0;
+  for (long i = 0; i < g.cells(); ++i) {
+    F(i, F_EX) = F(i, F_EX) + (-cj * F(i, F_JFX));
+    F(i, F_EY) = F(i, F_EY) + (-cj * F(i, F_JFY));
+    F(i, F_EZ) = F(i, F_EZ) + (-cj * F(i, F_JFZ));
+  }
+}
+
+template <class R>
+double es_energy(const R* fields, const Grid& g) {
+  CellSoA<R, kFieldMembers> F{const_cast<R*>(fields)};
+  double e = 0;
+  for (long i = 0; i < g.cells(); ++i) {
+    const double a = F(i, F_EX), b = F(i, F_EY), c = F(i, F_EZ);
+    e += a * a + b * b + c * c;
+  }
+  return 0.5 * e;
 }
 
 // e_energy / b_energy, src/fields.h:556-615: 0.5 * sum over the interior of
@@ -684,7 +747,11 @@ int orc_push_omp_f64(void* particles, int64_t n, int32_t vl, const double* inter
   int orc_current_fold_##SUF(T* fields, const orc_grid* gp) {                                \
     ORC_GRID(gp); orc::current_fold<T>(fields, g); return 0; }                              \
   int orc_ghost_copy_##SUF(T* fields, const orc_grid* gp, int32_t first_member) {            \
-    ORC_GRID(gp); orc::ghost_copy<T>(fields, g, first_member); return 0; }
+    ORC_GRID(gp); orc::ghost_copy<T>(fields, g, first_member); return 0; }                  \
+  int orc_es_advance_e_##SUF(T* fields, const orc_grid* gp, T dt_eps0, int32_t fold) {       \
+    ORC_GRID(gp); orc::es_advance_e<T>(fields, g, dt_eps0, fold != 0); return 0; }          \
+  double orc_es_energy_##SUF(const T* fields, const orc_grid* gp) {                          \
+    ORC_GRID(gp); return orc::es_energy<T>(fields, g); }
 
 ORC_FIELD_FNS(float, f32)
 ORC_FIELD_FNS(double, f64)
@@ -711,6 +778,18 @@ int orc_run_two_stream_em(int32_t precision, int32_t steps, int32_t vl, int32_t 
   if (precision == 4) return orc::run_two_stream_em<float>(steps, vl, literal != 0, out, params_out);
   if (precision == 8) return orc::run_two_stream_em<double>(steps, vl, literal != 0, out, params_out);
   return -1;
+}
+
+int orc_uncenter_f32(void* particles, int64_t n, int32_t vl, const float* interp, float qdt_2mc) {
+  orc::Particles<float> P{(unsigned char*)particles, vl};
+  orc::uncenter<float>(P, (size_t)n, interp, qdt_2mc);
+  return 0;
+}
+
+int orc_uncenter_f64(void* particles, int64_t n, int32_t vl, const double* interp, double qdt_2mc) {
+  orc::Particles<double> P{(unsigned char*)particles, vl};
+  orc::uncenter<double>(P, (size_t)n, interp, qdt_2mc);
+  return 0;
 }
 
 int orc_num_threads(void) {

@@ -47,9 +47,14 @@ class Oracle:
             getattr(lib, f"orc_energies_{suf}").argtypes = [_c_p, gp, _c_p]
             getattr(lib, f"orc_current_fold_{suf}").argtypes = [_c_p, gp]
             getattr(lib, f"orc_ghost_copy_{suf}").argtypes = [_c_p, gp, _i32]
+            getattr(lib, f"orc_es_advance_e_{suf}").argtypes = [_c_p, gp, real, _i32]
+            getattr(lib, f"orc_es_energy_{suf}").argtypes = [_c_p, gp]
+            getattr(lib, f"orc_es_energy_{suf}").restype = _f64
             getattr(lib, f"orc_default_particle_init_{suf}").argtypes = [
                 _c_p, _i64, _i32, _i64, _i64, real, _i64, real, real]
         lib.orc_run_two_stream_em.argtypes = [_i32, _i32, _i32, _i32, _c_p, _c_p]
+        lib.orc_uncenter_f32.argtypes = [_c_p, _i64, _i32, _c_p, _f32]
+        lib.orc_uncenter_f64.argtypes = [_c_p, _i64, _i32, _c_p, _f64]
         lib.orc_num_threads.restype = _i32
 
     @staticmethod
@@ -110,6 +115,15 @@ class Oracle:
     def default_particle_init(self, particles, n, vl, nx, ny, dxp, nppc, w, v0, dtype):
         getattr(self.lib, f"orc_default_particle_init_{self._suf(dtype)}")(
             _ptr(particles), n, vl, nx, ny, dxp, nppc, w, v0)
+
+    def es_advance_e(self, fields, g, dt_eps0, fold=True):
+        getattr(self.lib, f"orc_es_advance_e_{self._suf(fields.dtype)}")(_ptr(fields), C.byref(g), dt_eps0, int(fold))
+
+    def es_energy(self, fields, g) -> float:
+        return getattr(self.lib, f"orc_es_energy_{self._suf(fields.dtype)}")(_ptr(fields), C.byref(g))
+
+    def uncenter(self, particles, n, vl, interp, qdt_2mc):
+        getattr(self.lib, f"orc_uncenter_{self._suf(interp.dtype)}")(_ptr(particles), n, vl, _ptr(interp), qdt_2mc)
 
     # ---- whole runs -----------------------------------------------------
     def run_two_stream_em(self, steps: int, precision: int = 8, vl: int = 32, literal: bool = True):

@@ -107,3 +107,24 @@ def test_clear_and_initialize(orc):
     I.buf.fill_(1.0)
     pic.initialize_interpolator(I)
     assert float(I.buf.abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("real", [np.float32, np.float64])
+@pytest.mark.parametrize("fold", [True, False])
+@pytest.mark.parametrize("g", [(16, 1, 1), (7, 5, 6)])
+def test_es_solver(orc, g, real, fold):
+    """ES_Field_Solver(_1D)::advance_e and e_energy against the oracle."""
+    from cabanapic_gb300 import pic
+    nx, ny, nz = g
+    f, nc = random_fields(nx, ny, nz, seed=11, real=real)
+    F = _dev_fields(f, nc, real)
+    s = pic.ESFieldSolver1D(one_d=fold)
+    cj = real(0.37)
+    s.advance_e(F, 0, 0, 0, nx, ny, nz, 1, cj)
+    ref = f.copy()
+    orc.es_advance_e(ref, orc.grid(nx, ny, nz), cj, fold)
+    assert np.array_equal(F.buf.cpu().numpy(), ref)
+    e = s.e_energy(F, 0, 0, 0, nx, ny, nz, 1)
+    assert abs(e / orc.es_energy(ref, orc.grid(nx, ny, nz)) - 1) < 1e-13
+    s.advance_b(F, 0, 0, 0, nx, ny, nz, 1)  # a no-op in the reference
+    assert np.array_equal(F.buf.cpu().numpy(), ref)

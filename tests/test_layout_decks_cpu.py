@@ -83,3 +83,19 @@ def test_courant_length():
     cl = decks.courant_length(1.0, 2.0, 3.0, 10, 20, 30, R)
     w = (10 / 1.0) ** 2 + (20 / 2.0) ** 2 + (30 / 3.0) ** 2
     assert abs(float(cl) - (1 / w) ** 0.5) < 1e-7
+
+
+def test_product_energy_rule_matches_the_oracle_restatement(orc):
+    """cabanapic_gb300.energies (user-facing) against oracle.energy_rule on the
+    reference's gold files and the oracle's own history."""
+    from cabanapic_gb300 import energies
+    from conftest import gold_path
+    from oracle import energy_rule
+    out, par = orc.run_two_stream_em(6000, 8)
+    ours = energies.history_lines(out[:, :2], par["dt"])
+    assert ours == energy_rule.format_history(out[:, :2], par["dt"])
+    for kind in ("float", "double"):
+        gold = open(gold_path(kind)).read().splitlines()
+        (pe, ee, le), (pb, eb, lb) = energies.two_stream_em_rule(gold, ours)
+        (qe, fe, me, _), (qb, fb, mb, _) = energy_rule.two_stream_em_check(gold, ours)
+        assert (pe, pb) == (qe, qb) and (ee, eb) == (fe, fb) and (le, lb) == (me, mb)

@@ -67,3 +67,24 @@ def test_compare_error_absolute_branch():
     assert ok and err == 1e-17
     ok, _ = energy_rule.compare_error(0.0, 1e-15, 0.1)
     assert not ok
+
+
+@pytest.mark.parametrize("fold", [False, True])
+def test_oracle_es_solver_restates_the_reference(orc, fold):
+    """src/fields.h:400-436 / 511-544: E -= cj J over every cell (ghosts
+    included); the 1-D variant folds the jf ghosts first."""
+    from support import random_fields
+    nx, ny, nz = 9, 1, 1
+    f, nc = random_fields(nx, ny, nz, seed=4, real=np.float64)
+    g = orc.grid(nx, ny, nz)
+    got = f.copy()
+    orc.es_advance_e(got, g, 0.25, fold)
+    src = f.copy()
+    if fold:
+        orc.current_fold(src, g)
+    from cabanapic_gb300 import layout as L
+    v = L.unpack_cells(src, nc, 9)
+    v[:, 0:3] -= 0.25 * v[:, 6:9]
+    assert np.allclose(L.unpack_cells(got, nc, 9), v, rtol=0, atol=1e-15)
+    e = L.unpack_cells(got, nc, 9)[:, 0:3]
+    assert abs(orc.es_energy(got, g) - 0.5 * (e ** 2).sum()) < 1e-12 * (e ** 2).sum()
