@@ -38,6 +38,7 @@ sys.path.insert(0, ROOT)
 SORT_INTERVAL = 20
 N_CELLS = 128
 PPC = 64
+TILES = True
 # algorithmic bytes of push+deposit: per particle read 7 reals + cell, write 6
 # reals; per interior cell the 18 interpolator coefficients and 12 accumulators
 BYTES_PER_PARTICLE = {4: 56, 8: 108}
@@ -160,7 +161,7 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     if host_packed is None:
         host_packed = decks.thermal_particles(deck, packed=True)
     sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup,
-                     exact=exact)
+                     exact=exact, tiles=TILES)
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
         sim.step()
@@ -199,7 +200,7 @@ def e2e_run(precision, steps, warmup, host_packed, ws):
     pinned_out = torch.empty_like(pinned_in).pin_memory()
     energies_host = torch.empty((steps, 2), dtype=torch.float64).pin_memory()
     # warm-up on the same arrays (not timed), then reset the state from the host
-    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup)
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup, tiles=TILES)
     for _ in range(warmup):
         sim.step()
     torch.cuda.synchronize()
@@ -271,7 +272,7 @@ def cpu_sample_run(steps, warmup, precision=4, sample_ppc=8, threads=0):
 
 # ---------------------------------------------------------------- main
 def main():
-    global N_CELLS, PPC
+    global N_CELLS, PPC, TILES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -283,8 +284,10 @@ def main():
     ap.add_argument("--no-exact", action="store_true")
     ap.add_argument("--cells", type=int, default=N_CELLS, help="cells per axis (profiling cases)")
     ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (profiling cases)")
+    ap.add_argument("--streaming", action="store_true",
+                    help="streaming push kernel instead of the tiled one (comparison runs)")
     args = ap.parse_args()
-    N_CELLS, PPC = args.cells, args.ppc
+    N_CELLS, PPC, TILES = args.cells, args.ppc, not args.streaming
     ws, rank, local = _dist()
     metric = "particle-pushes/s (full step, FP32)"
     unit = "particle-pushes/s"
@@ -374,7 +377,8 @@ def main():
             "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload, "particles": n, "cells": deck.num_cells,
-                       "l2": "particle list 4.3 GB > L2: no flush needed", "replicas": ws},
+                       "l2": f"particle list {n * 32 / 1e9:.2f} GB > 129 MB L2: no flush needed",
+                       "replicas": ws, "push_kernel": "tiled" if TILES else "streaming"},
             "push_ms": push_ms,
             "push_ms_by_step": [round(t, 4) for t in res["push_ms"]],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -27,6 +27,7 @@ CPIC_FLOAT = 4
 CPIC_DOUBLE = 8
 CPIC_PUSH_TRUE_SQRT = 1
 CPIC_PUSH_EXACT = 2
+CPIC_PUSH_STREAMING = 4
 
 _vp = C.c_void_p
 _i64 = C.c_int64

@@ -12,29 +12,41 @@
 //                 exact arithmetic to ~1e-6 relative (tested at the 1e-5
 //                 tolerance stated for FP32).
 //
-// Design (one CUDA thread per particle, one warp per 32-particle AoSoA chunk):
-//   * a warp streams 32-particle chunks: with VL = 32 a chunk is one
-//     contiguous 1 KiB AoSoA block (128 B per member), with VL = 16 two; each
-//     lane's byte offsets inside a chunk are loop-invariant, and the next
-//     chunk's eight members are loaded before the current chunk is processed
-//     (one chunk of register prefetch per warp).  A ring of bulk asynchronous
-//     copies (cp.async.bulk into shared memory, four chunks ahead) was
-//     measured slower: it cut the latency stalls but added instructions and,
-//     with 200 KB of shared memory per SM, left too little L1 for the
-//     interpolator gathers;
-//   * the 18 interpolator coefficients of the particle's cell are gathered
-//     through the read-only cache; after a cell sort a warp mostly shares one
-//     cell, so the gather is a broadcast;
-//   * in-cell particles deposit their 12 currents through a warp reduction:
-//     when every depositing lane of the warp is in one cell, a 13-shuffle
-//     reduce-scatter leaves one total per lane and 12 lanes write it with one
-//     atomic each;
-//     otherwise the largest group of lanes sharing a cell is reduced that way
-//     and the other lanes use 16-byte vector reductions (red.global.add.v4);
-//   * cell-crossing particles are compacted into a per-warp shared-memory
-//     queue (ballot + prefix popcount) and moved 32 at a time, so the common
-//     path stays branch-free and the streak loop runs on full warps.  The
-//     streak loop is capped; hitting the cap sets CPIC_STATUS_MOVER_CAP.
+// Two kernels share the per-particle arithmetic (one CUDA thread per particle,
+// one warp per 32-particle AoSoA chunk, the next chunk's eight members held in
+// registers while the current one is processed):
+//
+//   push_kernel (CPIC_PUSH_STREAMING).  Warps stream 32-particle chunks: 18 read-only
+//   gathers per particle; in-cell deposits are reduced by shuffles over the
+//   largest group of lanes sharing a cell (all of them once particles are in
+//   cell order: a 13-shuffle reduce-scatter leaves 12 totals for 12 lanes,
+//   one atomic each), the other lanes use 16-byte vector reductions
+//   (red.global.add.v4.f32).
+//   push_tiled_kernel (default).  A CTA takes tiles of
+//   32 * 8 * chunks_per_warp consecutive particles.  Once particles are in cell
+//   order a tile covers a short run of voxels [lo, hi]; its cell window is that
+//   run widened by one voxel on each side (the segment [c0, c0 + wx)) together
+//   with the eight segments offset by +-1 in y and z (strides sx, sx*sy): 9
+//   segments, every cell a particle of the tile reaches some steps after a
+//   sort.  The 18 interpolator coefficients of the window's cells are staged in
+//   shared memory (rows of 20 values, 16-byte aligned) by cp.async copies
+//   issued one tile ahead (two buffers), so a gather is five vector shared
+//   loads instead of 18 dependent global loads.  A particle whose cell has no
+//   slot gathers from global memory, so results do not depend on the order,
+//   only the speed does.  The window is anchored on the median of 32 sampled
+//   cells of the tile, computed by warp 0 two tiles ahead.  Deposits as in
+//   push_kernel.  (A shared accumulator window was measured slower: shared
+//   float atomics are compare-and-swap loops, and the global reductions of
+//   reduced groups are cheap.)
+//
+// In both, cell-crossing particles are compacted into a per-warp shared-memory
+// queue (ballot + prefix popcount) holding the particle index and its
+// displacement; whenever 32 are queued the warp moves them together, so the
+// common path stays branch-free and the streak loop runs on full warps.  A
+// queued particle's offsets, weight and cell are still the ones in memory (an
+// in-cell particle's new offsets are stored, a crosser's are not) and are read
+// back when it is moved.  The streak loop is capped; hitting the cap sets
+// CPIC_STATUS_MOVER_CAP.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -53,18 +65,23 @@ struct PushArgs {
   GridDev g;
 };
 
+// Cell window of one tile: segments [c0 + off_s, c0 + off_s + wx) with
+// off_s = (s / 3 - 1) * sx * sy + (s % 3 - 1) * sx, s = 0..8.
+struct TileWin {
+  int c0, wx;
+};
+
 namespace CPIC_PUSH_NS {
 
 constexpr int kPushThreads = 256;
+constexpr int kWarps = kPushThreads / 32;
 constexpr int kQueueCap = 64;    // per warp: drained whenever it holds >= 32
 constexpr int kMaxStreaks = 16;  // a Courant-limited move needs at most 4
+constexpr int kRow = 20;         // window row: 18 coefficients + 2 pad
 
 template <class R>
 struct MoverQueue {
-  R px[kQueueCap], py[kQueueCap], pz[kQueueCap];  // offsets before the move
-  R dx[kQueueCap], dy[kQueueCap], dz[kQueueCap];  // normalised displacement
-  R q[kQueueCap];
-  int cell[kQueueCap];
+  R dx[kQueueCap], dy[kQueueCap], dz[kQueueCap];  // normalised half displacement
   int idx[kQueueCap];
 };
 
@@ -152,8 +169,8 @@ __device__ __forceinline__ int value_of_lane(int lane) {
   return ((lane & 16) ? 6 : 0) + ((lane & 8) ? 3 : 0) + j;
 }
 
-// Deposit of the in-cell particles of one warp.  `dep` lanes add v[0..11] to
-// accumulator row `cell`; `vi` is value_of_lane(lane).
+// Deposit of the in-cell particles of one warp into accumulator_array.  `dep`
+// lanes add v[0..11] to accumulator row `cell`; `vi` is value_of_lane(lane).
 template <class R>
 __device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool dep,
                                              const R v[12], int lane, int vi) {
@@ -192,13 +209,19 @@ __device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool
   }
 }
 
-// move_p for one particle (src/move_p.h:93-371), positions and displacement in
-// registers; writes the final offsets and cell of particle `pidx`.
+// move_p for one particle (src/move_p.h:93-371): reads the particle's offsets,
+// weight and cell (unchanged in memory for a crosser), runs the streaks with
+// the half displacement (dx, dy, dz) and writes the final offsets and cell.
 template <class R, int VL>
-__device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R py, R pz, R dx,
-                                      R dy, R dz, R q, int cell, int pidx, R* __restrict__ acc,
-                                      const GridDev g, int* __restrict__ status) {
+__device__ __noinline__ void move_one(unsigned char* __restrict__ part, R dx, R dy, R dz, int pidx,
+                                      R qsp, R* __restrict__ acc, const GridDev g,
+                                      int* __restrict__ status) {
   using L = PLayout<R, VL>;
+  R px = *reinterpret_cast<const R*>(part + L::off(pidx, 0));
+  R py = *reinterpret_cast<const R*>(part + L::off(pidx, 1));
+  R pz = *reinterpret_cast<const R*>(part + L::off(pidx, 2));
+  const R q = *reinterpret_cast<const R*>(part + L::off(pidx, 6)) * qsp;
+  int cell = *reinterpret_cast<const int*>(part + L::cell_off(pidx));
   if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) atomicOr(status, CPIC_STATUS_NONFINITE);
   bool done = false;
   for (int it = 0; it < kMaxStreaks; ++it) {
@@ -295,142 +318,410 @@ __device__ __forceinline__ void load_state(const unsigned char* __restrict__ chu
   }
 }
 
+// The 18 interpolator coefficients of one cell, in interpolator_array member
+// order (src/types.h interpolator members, src/push.h:74-93).
+template <class R>
+struct Coeffs {
+  R ex, dexdy, dexdz, d2exdydz;
+  R ey, deydz, deydx, d2eydzdx;
+  R ez, dezdx, dezdy, d2ezdxdy;
+  R cbx, dcbxdx, cby, dcbydy;
+  R cbz, dcbzdz;
+};
+
+template <class R>
+__device__ __forceinline__ void gather_global(const R* __restrict__ interp, int cell, Coeffs<R>& c) {
+  const R* f = interp + ((size_t)(cell >> 5) * (18 * kCellBlock) + (cell & 31));
+  c.ex = __ldg(f + 0 * 32); c.dexdy = __ldg(f + 1 * 32);
+  c.dexdz = __ldg(f + 2 * 32); c.d2exdydz = __ldg(f + 3 * 32);
+  c.ey = __ldg(f + 4 * 32); c.deydz = __ldg(f + 5 * 32);
+  c.deydx = __ldg(f + 6 * 32); c.d2eydzdx = __ldg(f + 7 * 32);
+  c.ez = __ldg(f + 8 * 32); c.dezdx = __ldg(f + 9 * 32);
+  c.dezdy = __ldg(f + 10 * 32); c.d2ezdxdy = __ldg(f + 11 * 32);
+  c.cbx = __ldg(f + 12 * 32); c.dcbxdx = __ldg(f + 13 * 32);
+  c.cby = __ldg(f + 14 * 32); c.dcbydy = __ldg(f + 15 * 32);
+  c.cbz = __ldg(f + 16 * 32); c.dcbzdz = __ldg(f + 17 * 32);
+}
+
+__device__ __forceinline__ void gather_row(const float* row, Coeffs<float>& c) {
+  const float4 a = *reinterpret_cast<const float4*>(row + 0);
+  const float4 b = *reinterpret_cast<const float4*>(row + 4);
+  const float4 d = *reinterpret_cast<const float4*>(row + 8);
+  const float4 e = *reinterpret_cast<const float4*>(row + 12);
+  const float2 f = *reinterpret_cast<const float2*>(row + 16);
+  c.ex = a.x; c.dexdy = a.y; c.dexdz = a.z; c.d2exdydz = a.w;
+  c.ey = b.x; c.deydz = b.y; c.deydx = b.z; c.d2eydzdx = b.w;
+  c.ez = d.x; c.dezdx = d.y; c.dezdy = d.z; c.d2ezdxdy = d.w;
+  c.cbx = e.x; c.dcbxdx = e.y; c.cby = e.z; c.dcbydy = e.w;
+  c.cbz = f.x; c.dcbzdz = f.y;
+}
+
+__device__ __forceinline__ void gather_row(const double* row, Coeffs<double>& c) {
+  const double2* r = reinterpret_cast<const double2*>(row);
+  double2 t;
+  t = r[0]; c.ex = t.x; c.dexdy = t.y;
+  t = r[1]; c.dexdz = t.x; c.d2exdydz = t.y;
+  t = r[2]; c.ey = t.x; c.deydz = t.y;
+  t = r[3]; c.deydx = t.x; c.d2eydzdx = t.y;
+  t = r[4]; c.ez = t.x; c.dezdx = t.y;
+  t = r[5]; c.dezdy = t.x; c.d2ezdxdy = t.y;
+  t = r[6]; c.cbx = t.x; c.dcbxdx = t.y;
+  t = r[7]; c.cby = t.x; c.dcbydy = t.y;
+  t = r[8]; c.cbz = t.x; c.dcbzdz = t.y;
+}
+
+// Field at the particle, relativistic Boris rotation with half E kicks
+// (push.h:124-163).  Updates (ux, uy, uz) in place.
+template <class R, bool LITERAL, bool FAST>
+__device__ __forceinline__ void boris(const Coeffs<R>& c, R x, R y, R z, R& ux, R& uy, R& uz,
+                                      const R qdt_2mc) {
+  const R one = 1., one_third = 1. / 3., two_fifteenths = 2. / 15.;
+  const R hax = qdt_2mc * ((c.ex + y * c.dexdy) + z * (c.dexdz + y * c.d2exdydz));
+  const R hay = qdt_2mc * ((c.ey + z * c.deydz) + x * (c.deydx + z * c.d2eydzdx));
+  const R haz = qdt_2mc * ((c.ez + x * c.dezdx) + y * (c.dezdy + x * c.d2ezdxdy));
+  const R cbx = c.cbx + x * c.dcbxdx;
+  const R cby = c.cby + y * c.dcbydy;
+  const R cbz = c.cbz + z * c.dcbzdz;
+  ux += hax; uy += hay; uz += haz;
+  const R b0 = scaled_rgamma<R, LITERAL, FAST>(qdt_2mc, one + (ux * ux + (uy * uy + uz * uz)));
+  const R b1 = cbx * cbx + (cby * cby + cbz * cbz);
+  const R b2 = (b0 * b0) * b1;
+  const R b3 = b0 * (one + b2 * (one_third + b2 * two_fifteenths));
+  R b4 = quotient<R, FAST>(b3, one + b1 * (b3 * b3));
+  b4 += b4;
+  const R tx = ux + b3 * (uy * cbz - uz * cby);
+  const R ty = uy + b3 * (uz * cbx - ux * cbz);
+  const R tz = uz + b3 * (ux * cby - uy * cbx);
+  ux += b4 * (ty * cbz - tz * cby);
+  uy += b4 * (tz * cbx - tx * cbz);
+  uz += b4 * (tx * cby - ty * cbx);
+  ux += hax; uy += hay; uz += haz;
+}
+
+// Per-warp constants of the chunk loop.
+struct LaneCtx {
+  int lane, vi, lane_off, lane_cell_off;
+  unsigned lt_mask;
+};
+
+__device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, int zs);
+
+// One 32-particle chunk: gather, Boris, in-cell move and deposit, queueing of
+// the crossers.  TILED gathers from the shared-memory window `wbuf` when the
+// particle's cell has a slot in window `w`.
+template <class R, int VL, bool LITERAL, bool FAST, bool TILED>
+__device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int n, int chunk,
+                                           const PState<R>& cur, const R* __restrict__ interp,
+                                           R* __restrict__ acc, const PushArgs<R>& a,
+                                           int* __restrict__ status, MoverQueue<R>& Q, int& qn,
+                                           const LaneCtx& lc, const R* __restrict__ wbuf,
+                                           const TileWin& w, int ys, int zs) {
+  constexpr int kMem = VL * (int)sizeof(R);
+  constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
+  const R one = 1., one_third = 1. / 3.;
+  unsigned char* base = part + (size_t)chunk * kChunk;
+  const int p = chunk * 32 + lc.lane;
+  bool valid = p < n;
+  const R x = cur.x, y = cur.y, z = cur.z;
+  R ux = cur.ux, uy = cur.uy, uz = cur.uz;
+  int cell = cur.cell;
+  if (valid && (unsigned)cell >= (unsigned)a.g.num_cells) {
+    atomicOr(status, CPIC_STATUS_CELL_RANGE);
+    valid = false;
+    cell = 0;
+  }
+  Coeffs<R> c;
+  int li = -1;
+  if constexpr (TILED) {
+    li = valid ? window_slot(cell, w, ys, zs) : -1;
+    if (li >= 0) gather_row(wbuf + li * kRow, c);
+    else gather_global<R>(interp, cell, c);
+  } else {
+    gather_global<R>(interp, cell, c);
+  }
+  boris<R, LITERAL, FAST>(c, x, y, z, ux, uy, uz, a.qdt_2mc);
+  if (valid) {
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 3 * kMem), ux);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 4 * kMem), uy);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 5 * kMem), uz);
+  }
+
+  // normalised half displacement and the in-cell test (push.h:169-187)
+  const R rg = scaled_rgamma<R, LITERAL, FAST>(one, one + (ux * ux + (uy * uy + uz * uz)));
+  ux *= a.cdt_dx; uy *= a.cdt_dy; uz *= a.cdt_dz;
+  ux *= rg; uy *= rg; uz *= rg;
+  const R mx = x + ux, my = y + uy, mz = z + uz;
+  const R nx = mx + ux, ny = my + uy, nz = mz + uz;
+  const R q = cur.w * a.qsp;
+  const bool inb = valid && (nx <= one && ny <= one && nz <= one && -nx <= one && -ny <= one &&
+                             -nz <= one);
+  if (inb) {
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 0 * kMem), nx);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 1 * kMem), ny);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 2 * kMem), nz);
+  }
+  R v[12];
+  const R corr = q * ux * uy * uz * one_third;
+  currents12<R>(q, ux, uy, uz, mx, my, mz, corr, v);
+  warp_deposit<R>(acc, cell, inb, v, lc.lane, lc.vi);
+
+  // compact the cell-crossing particles into the warp queue
+  const bool cross = valid && !inb;
+  const unsigned cm = __ballot_sync(kFull, cross);
+  if (cm) {
+    if (cross) {
+      const int s = qn + __popc(cm & lc.lt_mask);
+      Q.dx[s] = ux; Q.dy[s] = uy; Q.dz[s] = uz;
+      Q.idx[s] = p;
+    }
+    qn += __popc(cm);
+    if (qn >= 32) {
+      __syncwarp();
+      const int s = qn - 32 + lc.lane;
+      const R ddx = Q.dx[s], ddy = Q.dy[s], ddz = Q.dz[s];
+      const int ii = Q.idx[s];
+      __syncwarp();
+      qn -= 32;
+      move_one<R, VL>(part, ddx, ddy, ddz, ii, a.qsp, acc, a.g, status);
+    }
+  }
+}
+
+template <class R, int VL>
+__device__ __forceinline__ LaneCtx make_lane_ctx() {
+  constexpr int kBlk = VL * (7 * (int)sizeof(R) + (int)sizeof(int));
+  constexpr int kMem = VL * (int)sizeof(R);
+  LaneCtx lc;
+  lc.lane = (int)lane_id();
+  lc.lt_mask = (1u << lc.lane) - 1u;
+  lc.vi = value_of_lane(lc.lane);
+  lc.lane_off = (lc.lane / VL) * kBlk + (lc.lane % VL) * (int)sizeof(R);
+  lc.lane_cell_off = (lc.lane / VL) * kBlk + 7 * kMem + (lc.lane % VL) * (int)sizeof(int);
+  return lc;
+}
+
+template <class R, int VL>
+__device__ __forceinline__ void drain_queue(unsigned char* __restrict__ part, MoverQueue<R>& Q, int qn,
+                                            int lane, const PushArgs<R>& a, R* __restrict__ acc,
+                                            int* __restrict__ status) {
+  __syncwarp();
+  if (lane < qn) move_one<R, VL>(part, Q.dx[lane], Q.dy[lane], Q.dz[lane], Q.idx[lane], a.qsp, acc, a.g, status);
+}
+
+// ------------------------------------------------------------ streaming kernel
 template <class R, int VL, bool LITERAL, bool FAST>
 __global__ void __launch_bounds__(kPushThreads)
 push_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
             R* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status) {
-  constexpr size_t kBlk = (size_t)VL * (7 * sizeof(R) + sizeof(int));  // SoA block bytes
-  constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));  // 32 particles
-  constexpr int kMem = VL * (int)sizeof(R);
-  __shared__ MoverQueue<R> queues[kPushThreads / 32];
+  constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
+  __shared__ MoverQueue<R> queues[kWarps];
   MoverQueue<R>& Q = queues[threadIdx.x >> 5];
-  const int lane = lane_id();
-  const unsigned lt_mask = (1u << lane) - 1u;
-  const int vi = value_of_lane(lane);
-  // this lane's byte offsets inside a 32-particle chunk (loop-invariant)
-  const int lane_off = (lane / VL) * (int)kBlk + (lane % VL) * (int)sizeof(R);
-  const int lane_cell_off = (lane / VL) * (int)kBlk + 7 * kMem + (lane % VL) * (int)sizeof(int);
+  const LaneCtx lc = make_lane_ctx<R, VL>();
   const int nchunks = (n + 31) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const R one = 1., one_third = 1. / 3., two_fifteenths = 2. / 15.;
+  const TileWin nowin{0, 0};
   int qn = 0;
 
   int chunk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   PState<R> cur;
-  load_state<R, VL>(part + (size_t)chunk * kChunk, lane_off, lane_cell_off,
-                    chunk < nchunks && chunk * 32 + lane < n, cur);
+  load_state<R, VL>(part + (size_t)chunk * kChunk, lc.lane_off, lc.lane_cell_off,
+                    chunk < nchunks && chunk * 32 + lc.lane < n, cur);
   for (; chunk < nchunks; chunk += nwarps) {
-    // prefetch the next chunk of this warp
     const int next = chunk + nwarps;
     PState<R> nxt;
-    load_state<R, VL>(part + (size_t)next * kChunk, lane_off, lane_cell_off,
-                      next < nchunks && next * 32 + lane < n, nxt);
-
-    unsigned char* base = part + (size_t)chunk * kChunk;
-    const int p = chunk * 32 + lane;
-    bool valid = p < n;
-    const R x = cur.x, y = cur.y, z = cur.z;
-    R ux = cur.ux, uy = cur.uy, uz = cur.uz;
-    int cell = cur.cell;
-    if (valid && (unsigned)cell >= (unsigned)a.g.num_cells) {
-      atomicOr(status, CPIC_STATUS_CELL_RANGE);
-      valid = false;
-      cell = 0;
-    }
-    // gather (push.h:74-93)
-    const R* f = interp + ((size_t)(cell >> 5) * (18 * kCellBlock) + (cell & 31));
-    const R ex = __ldg(f + 0 * 32), dexdy = __ldg(f + 1 * 32);
-    const R dexdz = __ldg(f + 2 * 32), d2exdydz = __ldg(f + 3 * 32);
-    const R ey = __ldg(f + 4 * 32), deydz = __ldg(f + 5 * 32);
-    const R deydx = __ldg(f + 6 * 32), d2eydzdx = __ldg(f + 7 * 32);
-    const R ez = __ldg(f + 8 * 32), dezdx = __ldg(f + 9 * 32);
-    const R dezdy = __ldg(f + 10 * 32), d2ezdxdy = __ldg(f + 11 * 32);
-    R cbx = __ldg(f + 12 * 32);
-    const R dcbxdx = __ldg(f + 13 * 32);
-    R cby = __ldg(f + 14 * 32);
-    const R dcbydy = __ldg(f + 15 * 32);
-    R cbz = __ldg(f + 16 * 32);
-    const R dcbzdz = __ldg(f + 17 * 32);
-
-    // field at the particle (push.h:124-138)
-    const R hax = a.qdt_2mc * ((ex + y * dexdy) + z * (dexdz + y * d2exdydz));
-    const R hay = a.qdt_2mc * ((ey + z * deydz) + x * (deydx + z * d2eydzdx));
-    const R haz = a.qdt_2mc * ((ez + x * dezdx) + y * (dezdy + x * d2ezdxdy));
-    cbx = cbx + x * dcbxdx;
-    cby = cby + y * dcbydy;
-    cbz = cbz + z * dcbzdz;
-
-    // relativistic Boris rotation with half E kicks (push.h:144-163)
-    ux += hax; uy += hay; uz += haz;
-    const R b0 = scaled_rgamma<R, LITERAL, FAST>(a.qdt_2mc, one + (ux * ux + (uy * uy + uz * uz)));
-    const R b1 = cbx * cbx + (cby * cby + cbz * cbz);
-    const R b2 = (b0 * b0) * b1;
-    const R b3 = b0 * (one + b2 * (one_third + b2 * two_fifteenths));
-    R b4 = quotient<R, FAST>(b3, one + b1 * (b3 * b3));
-    b4 += b4;
-    const R tx = ux + b3 * (uy * cbz - uz * cby);
-    const R ty = uy + b3 * (uz * cbx - ux * cbz);
-    const R tz = uz + b3 * (ux * cby - uy * cbx);
-    ux += b4 * (ty * cbz - tz * cby);
-    uy += b4 * (tz * cbx - tx * cbz);
-    uz += b4 * (tx * cby - ty * cbx);
-    ux += hax; uy += hay; uz += haz;
-    if (valid) {
-      __stcs(reinterpret_cast<R*>(base + lane_off + 3 * kMem), ux);
-      __stcs(reinterpret_cast<R*>(base + lane_off + 4 * kMem), uy);
-      __stcs(reinterpret_cast<R*>(base + lane_off + 5 * kMem), uz);
-    }
-
-    // normalised half displacement and the in-cell test (push.h:169-187)
-    const R rg = scaled_rgamma<R, LITERAL, FAST>(one, one + (ux * ux + (uy * uy + uz * uz)));
-    ux *= a.cdt_dx; uy *= a.cdt_dy; uz *= a.cdt_dz;
-    ux *= rg; uy *= rg; uz *= rg;
-    const R mx = x + ux, my = y + uy, mz = z + uz;
-    const R nx = mx + ux, ny = my + uy, nz = mz + uz;
-    const R q = cur.w * a.qsp;
-    const bool inb = valid && (nx <= one && ny <= one && nz <= one && -nx <= one && -ny <= one &&
-                               -nz <= one);
-    if (inb) {
-      __stcs(reinterpret_cast<R*>(base + lane_off + 0 * kMem), nx);
-      __stcs(reinterpret_cast<R*>(base + lane_off + 1 * kMem), ny);
-      __stcs(reinterpret_cast<R*>(base + lane_off + 2 * kMem), nz);
-    }
-    R v[12];
-    const R corr = q * ux * uy * uz * one_third;
-    currents12<R>(q, ux, uy, uz, mx, my, mz, corr, v);
-    warp_deposit<R>(acc, cell, inb, v, lane, vi);
-
-    // compact the cell-crossing particles into the warp queue
-    const bool cross = valid && !inb;
-    const unsigned cm = __ballot_sync(kFull, cross);
-    if (cm) {
-      if (cross) {
-        const int s = qn + __popc(cm & lt_mask);
-        Q.px[s] = x; Q.py[s] = y; Q.pz[s] = z;
-        Q.dx[s] = ux; Q.dy[s] = uy; Q.dz[s] = uz;
-        Q.q[s] = q; Q.cell[s] = cell; Q.idx[s] = p;
-      }
-      qn += __popc(cm);
-      if (qn >= 32) {
-        __syncwarp();
-        const int s = qn - 32 + lane;
-        const R ex0 = Q.px[s], ey0 = Q.py[s], ez0 = Q.pz[s];
-        const R ddx = Q.dx[s], ddy = Q.dy[s], ddz = Q.dz[s], qq = Q.q[s];
-        const int cc = Q.cell[s], ii = Q.idx[s];
-        __syncwarp();
-        qn -= 32;
-        move_one<R, VL>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, status);
-      }
-    }
+    load_state<R, VL>(part + (size_t)next * kChunk, lc.lane_off, lc.lane_cell_off,
+                      next < nchunks && next * 32 + lc.lane < n, nxt);
+    push_chunk<R, VL, LITERAL, FAST, false>(part, n, chunk, cur, interp, acc, a, status, Q, qn, lc,
+                                            nullptr, nowin, 0, 0);
     cur = nxt;
   }
-  __syncwarp();
-  if (lane < qn) {
-    move_one<R, VL>(part, Q.px[lane], Q.py[lane], Q.pz[lane], Q.dx[lane], Q.dy[lane], Q.dz[lane],
-                    Q.q[lane], Q.cell[lane], Q.idx[lane], acc, a.g, status);
+  drain_queue<R, VL>(part, Q, qn, lc.lane, a, acc, status);
+}
+
+// ------------------------------------------------------------ tiled kernel
+// Slot of `cell` in the window, or -1.  With r = cell - c0 + sx*sy + sx the
+// window is r = dx + ky * ys + kz * zs, dx < wx <= ys, ky, kz in {0, 1, 2}.
+__device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, int zs) {
+  int r = cell - w.c0 + ys + zs;
+  if ((unsigned)r >= (unsigned)(3 * zs)) return -1;
+  const int kz = (r >= zs) + (r >= 2 * zs);
+  r -= kz * zs;
+  const int ky = (r >= ys) + (r >= 2 * ys);
+  r -= ky * ys;
+  return r < w.wx ? r + w.wx * (ky + 3 * kz) : -1;
+}
+
+// First voxel of window segment s (ky = s % 3, kz = s / 3).
+__device__ __forceinline__ int segment_start(const TileWin& w, int s, int ys, int zs) {
+  const int kz = s / 3, ky = s - 3 * kz;
+  return w.c0 + (kz - 1) * zs + (ky - 1) * ys;
+}
+
+// Window of a tile from the cells of 32 of its particles, one per lane (the
+// first particle of every 32nd part of the tile).  Some steps after a sort a
+// sampled particle may sit one cell away in y or z (a voxel index off by sx
+// or sx*sy), so the anchor is the median sample, and the run [lo, hi] is
+// taken over the samples within wxmax voxels of it.  Warp-uniform result.
+__device__ __forceinline__ TileWin window_from_samples(int c, int lane, int wxmax, int num_cells) {
+  if ((unsigned)c >= (unsigned)num_cells) c = 0;
+  int sorted = c;  // bitonic sort of the 32 samples, ascending over the lanes
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int o = __shfl_xor_sync(kFull, sorted, j);
+      const bool up = (lane & k) == 0;
+      const bool low = (lane & j) == 0;
+      sorted = (low == up) ? min(sorted, o) : max(sorted, o);
+    }
+  }
+  const int m = __shfl_sync(kFull, sorted, 16);
+  const bool near = c >= m - wxmax && c <= m + wxmax;
+  const int lo = __reduce_min_sync(kFull, near ? c : 0x7fffffff);
+  const int hi = __reduce_max_sync(kFull, near ? c : -1);
+  TileWin w;
+  if (hi - lo <= wxmax - 3) {
+    w.c0 = lo - 1;
+    w.wx = hi - lo + 3;
+  } else {
+    w.wx = wxmax;
+    w.c0 = m - (wxmax >> 1);
+  }
+  return w;
+}
+
+template <class R>
+__device__ __forceinline__ void cp_async_elem(R* dst_smem, const R* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  if constexpr (sizeof(R) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Window segment of slot i: s = floor(i / wx), exact in float for i < 9 * 64.
+__device__ __forceinline__ int slot_segment(int i, float inv_wx) {
+  return min((int)(((float)i + 0.5f) * inv_wx), 8);
+}
+
+// Issues the copies of the window's interpolator rows (one thread per window
+// cell, 18 asynchronous element copies); cells outside the array read as 0.
+template <class R>
+__device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __restrict__ interp,
+                                             const TileWin w, int ys, int zs, int num_cells) {
+  const int ncell = 9 * w.wx;
+  const float inv_wx = 1.0f / (float)w.wx;
+  for (int i = threadIdx.x; i < ncell; i += kPushThreads) {
+    const int s = slot_segment(i, inv_wx);
+    const int gc = segment_start(w, s, ys, zs) + (i - s * w.wx);
+    R* row = buf + i * kRow;
+    if ((unsigned)gc < (unsigned)num_cells) {
+      const R* src = interp + ((size_t)(gc >> 5) * (18 * kCellBlock) + (gc & 31));
+#pragma unroll
+      for (int m = 0; m < 18; ++m) cp_async_elem<R>(row + m, src + m * kCellBlock);
+    } else {
+#pragma unroll
+      for (int m = 0; m < 18; ++m) row[m] = R(0);
+    }
   }
 }
 
+// Shared memory of the tiled kernel beyond its static part: two interpolator
+// windows of 9 * wxmax cells.
+template <class R>
+constexpr size_t tiled_dyn_smem(int wxmax) {
+  return (size_t)9 * wxmax * 2 * kRow * sizeof(R);
+}
+
+// Cell of the lane-th sample particle of tile t (tiles of T particles).
+template <class R, int VL>
+__device__ __forceinline__ int tile_sample(const unsigned char* __restrict__ part, int n, int T, int t,
+                                           int lane) {
+  using L = PLayout<R, VL>;
+  int64_t p = (int64_t)t * T + (int64_t)lane * (T >> 5);
+  if (p > n - 1) p = n - 1;
+  return __ldcg(reinterpret_cast<const int*>(part + L::cell_off(p)));
+}
+
+template <class R, int VL, bool LITERAL, bool FAST>
+__global__ void __launch_bounds__(kPushThreads)
+push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
+                  R* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status,
+                  int chunks_per_warp, int wxmax) {
+  constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* const wbuf0 = reinterpret_cast<R*>(smem_raw);
+  R* const wbuf1 = wbuf0 + 9 * wxmax * kRow;
+  __shared__ MoverQueue<R> queues[kWarps];
+  __shared__ TileWin wins[3];
+  const int warp = threadIdx.x >> 5;
+  MoverQueue<R>& Q = queues[warp];
+  const LaneCtx lc = make_lane_ctx<R, VL>();
+  const int cpt = kWarps * chunks_per_warp;  // chunks per tile
+  const int T = 32 * cpt;                    // particles per tile
+  const int ntiles = (int)(((int64_t)n + T - 1) / T);
+  const int nchunks = (n + 31) >> 5;
+  const int ys = a.g.sx, zs = a.g.sx * a.g.sy, nc = a.g.num_cells;
+  const int G = gridDim.x;
+  int t = blockIdx.x;
+  if (t >= ntiles) return;
+
+  // prologue: warp 0 sets the windows of the first two tiles and loads the
+  // samples of the third
+  int sample = 0;
+  if (warp == 0) {
+    TileWin w0 = window_from_samples(tile_sample<R, VL>(part, n, T, t, lc.lane), lc.lane, wxmax, nc);
+    TileWin w1 = w0;
+    if (t + G < ntiles)
+      w1 = window_from_samples(tile_sample<R, VL>(part, n, T, t + G, lc.lane), lc.lane, wxmax, nc);
+    if (lc.lane == 0) { wins[0] = w0; wins[1] = w1; }
+    if (t + 2 * G < ntiles) sample = tile_sample<R, VL>(part, n, T, t + 2 * G, lc.lane);
+  }
+  __syncthreads();
+  stage_window<R>(wbuf0, interp, wins[0], ys, zs, nc);
+  cp_async_commit();
+
+  int qn = 0;
+  int chunk = t * cpt + warp;
+  PState<R> cur;
+  load_state<R, VL>(part + (size_t)chunk * kChunk, lc.lane_off, lc.lane_cell_off,
+                    chunk < nchunks && chunk * 32 + lc.lane < n, cur);
+  for (int j = 0; t < ntiles; ++j, t += G) {
+    cp_async_wait_all();
+    // window j staged by every thread; window j+1 published; every warp done
+    // reading the buffer that window j+1 is staged into
+    __syncthreads();
+    const TileWin w = wins[j % 3];
+    const R* const wb = (j & 1) ? wbuf1 : wbuf0;
+    const int t1 = t + G;
+    if (t1 < ntiles) {
+      stage_window<R>((j & 1) ? wbuf0 : wbuf1, interp, wins[(j + 1) % 3], ys, zs, nc);
+      cp_async_commit();
+    }
+    if (warp == 0 && t1 + G < ntiles) {
+      const TileWin w2 = window_from_samples(sample, lc.lane, wxmax, nc);
+      if (lc.lane == 0) wins[(j + 2) % 3] = w2;
+      if (t1 + 2 * G < ntiles) sample = tile_sample<R, VL>(part, n, T, t1 + 2 * G, lc.lane);
+    }
+    for (int i = 0; i < chunks_per_warp; ++i) {
+      chunk = t * cpt + warp + kWarps * i;
+      const bool last = i + 1 == chunks_per_warp;
+      const int next = last ? t1 * cpt + warp : chunk + kWarps;
+      PState<R> nxt;
+      load_state<R, VL>(part + (size_t)next * kChunk, lc.lane_off, lc.lane_cell_off,
+                        (!last || t1 < ntiles) && next < nchunks && next * 32 + lc.lane < n, nxt);
+      if (chunk < nchunks)
+        push_chunk<R, VL, LITERAL, FAST, true>(part, n, chunk, cur, interp, acc, a, status, Q, qn,
+                                               lc, wb, w, ys, zs);
+      cur = nxt;
+    }
+  }
+  drain_queue<R, VL>(part, Q, qn, lc.lane, a, acc, status);
+}
+
+// ------------------------------------------------------------ host side
 template <class R, int VL, bool LITERAL, bool FAST>
 int launch_push(void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
                 int* status, cudaStream_t s) {
@@ -445,7 +736,7 @@ int launch_push(void* particles, int n, const void* interp, void* acc, const Pus
   }
   const int64_t chunks = ((int64_t)n + 31) / 32;
   int64_t blocks = (int64_t)sm_count() * per_sm[dev];
-  const int64_t need = (chunks + kPushThreads / 32 - 1) / (kPushThreads / 32);
+  const int64_t need = (chunks + kWarps - 1) / kWarps;
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, kPushThreads, 0, s>>>(static_cast<unsigned char*>(particles), n,
@@ -454,24 +745,91 @@ int launch_push(void* particles, int n, const void* interp, void* acc, const Pus
   return launch_status();
 }
 
-// Dispatch over real_t, vector length and the sqrt variant.
+// Tile shape from the mean particles per interior cell: the largest tile
+// (up to 4 chunks per warp, 1024 particles) whose sorted run of cells, with
+// one voxel of margin each side, fits a window of at most 32 voxels.
+struct TileShape {
+  int chunks_per_warp, wxmax;
+};
+
+inline TileShape tile_shape(int64_t n, const GridDev& g) {
+  const double ppc = (double)n / ((double)g.nx * g.ny * g.nz);
+  TileShape ts{1, 32};
+  for (int cpw = 4; cpw >= 1; --cpw) {
+    const double cells = 32.0 * kWarps * cpw / (ppc > 1e-9 ? ppc : 1e-9);
+    const int wx = (int)(1.25 * cells) + 4;  // slack for cell-count fluctuations
+    if (wx <= 32 || cpw == 1) {
+      ts.chunks_per_warp = cpw;
+      ts.wxmax = wx < 32 ? wx : 32;
+      break;
+    }
+  }
+  if (ts.wxmax > g.sx) ts.wxmax = g.sx;  // segments of one window must not overlap
+  if (ts.wxmax < 3) ts.wxmax = 3;
+  return ts;
+}
+
+template <class R, int VL, bool LITERAL, bool FAST>
+int launch_push_tiled(void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
+                      int* status, cudaStream_t s) {
+  auto kern = push_tiled_kernel<R, VL, LITERAL, FAST>;
+  const TileShape ts = tile_shape(n, a.g);
+  const size_t dyn = tiled_dyn_smem<R>(ts.wxmax);
+  static size_t opted[64] = {0};
+  static size_t occ_dyn[64] = {0};
+  static int occ_blocks[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CPIC_ECUDA;
+  // the 48 KB default covers static + dynamic shared memory: opt in for any size
+  if (opted[dev] < dyn) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
+      return CPIC_ECUDA;
+    opted[dev] = dyn;
+  }
+  if (occ_dyn[dev] != dyn) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kPushThreads, dyn) != cudaSuccess || b < 1) b = 1;
+    occ_blocks[dev] = b;
+    occ_dyn[dev] = dyn;
+  }
+  const int64_t T = 32LL * kWarps * ts.chunks_per_warp;
+  const int64_t ntiles = ((int64_t)n + T - 1) / T;
+  int64_t blocks = (int64_t)sm_count() * occ_blocks[dev];
+  if (blocks > ntiles) blocks = ntiles;
+  if (blocks < 1) blocks = 1;
+  kern<<<(unsigned)blocks, kPushThreads, dyn, s>>>(static_cast<unsigned char*>(particles), n,
+                                                  static_cast<const R*>(interp), static_cast<R*>(acc), a,
+                                                  status, ts.chunks_per_warp, ts.wxmax);
+  return launch_status();
+}
+
+template <class R, int VL, bool LITERAL, bool FAST>
+int launch_any(bool tiled, void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
+               int* status, cudaStream_t s) {
+  return tiled ? launch_push_tiled<R, VL, LITERAL, FAST>(particles, n, interp, acc, a, status, s)
+               : launch_push<R, VL, LITERAL, FAST>(particles, n, interp, acc, a, status, s);
+}
+
+// Dispatch over real_t, vector length, the sqrt variant and the kernel.
 template <bool FAST>
 int push_dispatch(void* particles, int n, const void* interp, void* acc, const cpic_grid* g,
                   const cpic_push_params* prm, int* status, cudaStream_t s) {
   const bool literal = !(prm->flags & CPIC_PUSH_TRUE_SQRT);
   const GridDev gd = make_grid(g);
+  // the window arithmetic keeps 3 * sx * sy and cell + sx * sy + sx in int range
+  const bool tiled = !(prm->flags & CPIC_PUSH_STREAMING) && gd.num_cells <= (1 << 30);
   if (prm->precision == CPIC_FLOAT) {
     PushArgs<float> a{(float)prm->qdt_2mc, (float)prm->cdt_dx, (float)prm->cdt_dy,
                       (float)prm->cdt_dz, (float)prm->qsp, gd};
-    return prm->particle_vl == 32 ? launch_push<float, 32, true, FAST>(particles, n, interp, acc, a, status, s)
-                                  : launch_push<float, 16, true, FAST>(particles, n, interp, acc, a, status, s);
+    return prm->particle_vl == 32 ? launch_any<float, 32, true, FAST>(tiled, particles, n, interp, acc, a, status, s)
+                                  : launch_any<float, 16, true, FAST>(tiled, particles, n, interp, acc, a, status, s);
   }
   PushArgs<double> a{prm->qdt_2mc, prm->cdt_dx, prm->cdt_dy, prm->cdt_dz, prm->qsp, gd};
   if (prm->particle_vl == 32)
-    return literal ? launch_push<double, 32, true, FAST>(particles, n, interp, acc, a, status, s)
-                   : launch_push<double, 32, false, FAST>(particles, n, interp, acc, a, status, s);
-  return literal ? launch_push<double, 16, true, FAST>(particles, n, interp, acc, a, status, s)
-                 : launch_push<double, 16, false, FAST>(particles, n, interp, acc, a, status, s);
+    return literal ? launch_any<double, 32, true, FAST>(tiled, particles, n, interp, acc, a, status, s)
+                   : launch_any<double, 32, false, FAST>(tiled, particles, n, interp, acc, a, status, s);
+  return literal ? launch_any<double, 16, true, FAST>(tiled, particles, n, interp, acc, a, status, s)
+                 : launch_any<double, 16, false, FAST>(tiled, particles, n, interp, acc, a, status, s);
 }
 
 }  // namespace CPIC_PUSH_NS

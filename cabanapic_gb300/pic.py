@@ -74,15 +74,18 @@ def _grid(nx, ny, nz, ng, boundary=Boundary.Periodic):
 # ---------------------------------------------------------------- push
 def push(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp,
          a0: AccumulatorArray, g, nx, ny, nz, num_ghosts, boundary, *, true_sqrt: bool = False,
-         exact: bool = False, stream=None) -> None:
+         exact: bool = False, tiles: bool = True, stream=None) -> None:
     """push() (src/push.h:7-300): Boris push, move and current deposit.
 
     `g` (grid_t*) is accepted and unused, as in the reference.  Adds into a0.
     exact=True selects the bit-exact variant (unfused arithmetic, IEEE
     division and sqrtf); the default uses fused multiply-adds and the hardware
-    reciprocal square root (within 1e-5 relative per particle)."""
+    reciprocal square root (within 1e-5 relative per particle).  tiles=False
+    selects the streaming kernel (no shared-memory cell windows; same
+    results, slower once particles are in cell order)."""
     lib = capi.load()
-    flags = (capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0) | (capi.CPIC_PUSH_EXACT if exact else 0)
+    flags = ((capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0) | (capi.CPIC_PUSH_EXACT if exact else 0)
+             | (0 if tiles else capi.CPIC_PUSH_STREAMING))
     prm = capi.CpicPushParams(float(qdt_2mc), float(cdt_dx), float(cdt_dy), float(cdt_dz),
                               float(qsp), particles.precision, particles.vl, flags, 0)
     if f0.precision != particles.precision or a0.precision != particles.precision:

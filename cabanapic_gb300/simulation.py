@@ -19,7 +19,8 @@ from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleLis
 
 class Simulation:
     def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
-                 max_steps: int = None, time_push: bool = False, exact: bool = False):
+                 max_steps: int = None, time_push: bool = False, exact: bool = False,
+                 tiles: bool = True):
         self.deck = deck
         self.p = deck.derived()
         dev = torch.device(device if device is not None else "cuda")
@@ -43,6 +44,7 @@ class Simulation:
         self.time_push = time_push
         self.push_events = []
         self.exact = bool(exact)
+        self.tiles = bool(tiles)
 
     # ------------------------------------------------------------------
     def step(self) -> None:
@@ -57,7 +59,8 @@ class Simulation:
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
         pic.push(self.particles, self.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
-                 p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary, exact=self.exact)
+                 p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary, exact=self.exact,
+                 tiles=self.tiles)
         if self.time_push:
             e1.record()
             self.push_events.append((e0, e1))

@@ -59,6 +59,10 @@ typedef struct CUstream_st* cpic_stream_t;
                                   are bit-identical to a CPU build of the reference without
                                   FMA contraction.  Default (0): fused multiply-adds and the
                                   hardware reciprocal square root, within 1e-5 relative. */
+#define CPIC_PUSH_STREAMING 4  /* streaming kernel: per-particle global gathers, no
+                                  shared-memory cell window.  Same results as the default
+                                  tiled kernel, which is faster once particles are in cell
+                                  order. */
 
 /* Grid of the run: interior cells nx*ny*nz plus num_ghosts ghost layers;
  * boundary is the deck's BOUNDARY_TYPE, which the reference's field code reads

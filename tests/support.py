@@ -8,12 +8,15 @@ from cabanapic_gb300 import layout as L
 
 
 def random_state(nx=6, ny=5, nz=4, n=4000, seed=0, real=np.float32, crossing=0.3, vl=32,
-                 sort=False, cdt=(0.45, 0.40, 0.35), qdt_2mc=-0.05, edge_cases=True):
+                 sort=False, cdt=(0.45, 0.40, 0.35), qdt_2mc=-0.05, edge_cases=True, disorder=0.0):
     """Random interpolator + particles on an nx*ny*nz periodic grid.
 
     A fraction `crossing` of the particles gets large momenta (several face
     crossings per push); the rest move within their cell.  With edge_cases,
-    some particles sit exactly on faces or have zero momentum components."""
+    some particles sit exactly on faces or have zero momentum components.
+    With sort, particles are in cell order; `disorder` then moves that fraction
+    of them to a random neighbouring interior cell without reordering (the
+    state some steps after a sort)."""
     R = np.dtype(real).type
     rng = np.random.default_rng(seed)
     sx, sy, sz = nx + 2, ny + 2, nz + 2
@@ -40,6 +43,14 @@ def random_state(nx=6, ny=5, nz=4, n=4000, seed=0, real=np.float32, crossing=0.3
     if sort:
         order = np.argsort(cell, kind="stable")
         p = {k: v[order] for k, v in p.items()}
+    if disorder > 0:
+        moved = rng.random(n) < disorder
+        jx, jy, jz = L.rank_to_index(p["cell"], nx, ny)
+        d = rng.integers(-1, 2, (3, n))
+        jx = np.where(moved, (jx - 1 + d[0]) % nx + 1, jx)
+        jy = np.where(moved, (jy - 1 + d[1]) % ny + 1, jy)
+        jz = np.where(moved, (jz - 1 + d[2]) % nz + 1, jz)
+        p["cell"] = L.voxel(jx, jy, jz, nx, ny).astype(np.int32)
     p = {k: (v.astype(R) if k != "cell" else v) for k, v in p.items()}
     packed = L.pack_particles(p, R, vl)
     push_args = (R(qdt_2mc), R(cdt[0]), R(cdt[1]), R(cdt[2]), R(-1.0))

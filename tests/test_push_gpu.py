@@ -20,7 +20,7 @@ from support import assert_particles_close, random_state, reorder_bound  # noqa:
 pytestmark = pytest.mark.gpu
 
 
-def _run_pair(orc, st, true_sqrt=False, exact=True):
+def _run_pair(orc, st, true_sqrt=False, exact=True, tiles=True):
     from cabanapic_gb300 import pic
     R = st["real"]
     nc = st["num_cells"]
@@ -35,7 +35,7 @@ def _run_pair(orc, st, true_sqrt=False, exact=True):
     I.buf.copy_(torch.from_numpy(st["interp"]))
     A = pic.AccumulatorArray(nc, R)
     pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic,
-             true_sqrt=true_sqrt, exact=exact)
+             true_sqrt=true_sqrt, exact=exact, tiles=tiles)
     pic.check_status()
     return host, acc, acc_abs, cnt, P.download_bytes(), A.get(), crossers
 
@@ -67,6 +67,25 @@ def test_push_float_vl32(orc, sort, n):
     _assert_parity(_run_pair(orc, st, exact=False), np.float32, st, exact=False)
     if n >= 4000:
         assert res[-1] > 0.2 * n  # the crossing path was exercised
+
+
+@pytest.mark.parametrize("real,vl", [(np.float32, 32), (np.float32, 16), (np.float64, 32)])
+@pytest.mark.parametrize("disorder", [0.0, 0.6])
+def test_push_cell_window(orc, real, vl, disorder):
+    """Particles in cell order on 40-cell rows at 64 per cell: a tile's run of
+    cells fits the tiled kernel's shared-memory window, so window gathers serve
+    nearly every particle.  With disorder, 60% of them sit in a neighbouring
+    cell (as some steps after a sort): they still hit the window (one voxel of
+    margin, y and z neighbour segments) except at its edges, where the global
+    gather takes over.  Both kernels must match the oracle, and each other bit
+    for bit in particle state."""
+    st = random_state(nx=40, ny=3, nz=3, n=64 * 360, seed=7, real=real, vl=vl, sort=True,
+                      crossing=0.05, disorder=disorder)
+    _both(orc, st, real)
+    _both(orc, st, real, tiles=False)
+    tiled = _run_pair(orc, st, exact=False)
+    stream = _run_pair(orc, st, exact=False, tiles=False)
+    assert np.array_equal(tiled[4], stream[4])
 
 
 def test_push_float_vl16(orc):

@@ -57,8 +57,13 @@ def test_float_gpu_within_reordering_envelope(gpu_runs, orc):
     individual deposits, so the summation order of the deposit alone moves the
     energy history at the 1e-4 level.  The oracle run on randomly permuted
     particle orders (identical particles, different accumulation order) gives
-    that envelope; the GPU's atomics must stay within a small multiple of it."""
+    that envelope; the GPU's atomics must stay within a small multiple of it.
+    The GPU run uses the exact push variant, so that summation order is the
+    only difference (the default variant's fused multiply-adds perturb each
+    particle by ~1e-6 as well; its error is checked against the FP64 truth
+    below)."""
     from cabanapic_gb300 import decks, layout as L
+    from cabanapic_gb300.simulation import Simulation
     deck = decks.two_stream_em(precision=4, num_steps=200)
     host = decks.default_particles(deck)
     base = oracle_run(orc, deck, L.pack_particles(host, np.float32, 32), 200)
@@ -69,8 +74,10 @@ def test_float_gpu_within_reordering_envelope(gpu_runs, orc):
         ph = {k: v[perm] for k, v in host.items()}
         e = oracle_run(orc, deck, L.pack_particles(ph, np.float32, 32), 200)
         env = np.maximum(env, history_deviation(e, base))
-    gpu = gpu_runs[4][0][:200]
-    dev = history_deviation(gpu, base)
+    sim = Simulation(deck, exact=True)
+    sim.run(200)
+    sim.check_status()
+    dev = history_deviation(sim.energies(), base)
     assert np.all(env > 0)
     assert np.all(dev <= 3 * env), (dev, env)
 
