@@ -20,6 +20,7 @@ CPIC_ESCRATCH = -4
 CPIC_STATUS_CELL_RANGE = 1
 CPIC_STATUS_MOVER_CAP = 2
 CPIC_STATUS_NONFINITE = 4
+CPIC_STATUS_PIPELINE = 8
 
 CPIC_REFLECT = 0
 CPIC_PERIODIC = 1
@@ -66,6 +67,8 @@ class CpicDeviceError(RuntimeError):
             names.append("move_p streak cap reached")
         if bits & CPIC_STATUS_NONFINITE:
             names.append("non-finite particle displacement")
+        if bits & CPIC_STATUS_PIPELINE:
+            names.append("a bounded wait in the tiled push gave up")
         super().__init__("device status %#x: %s" % (bits, "; ".join(names) or "unknown"))
         self.bits = bits
 

@@ -61,6 +61,45 @@ __device__ __forceinline__ void red_add4(double* a, double v0, double v1, double
   atomicAdd(a + 0, v0); atomicAdd(a + 1, v1); atomicAdd(a + 2, v2); atomicAdd(a + 3, v3);
 }
 
+// ---- shared-memory mbarriers (CTA scope)
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+// Arrive (release): the caller's earlier shared-memory writes are visible to
+// threads that then observe the phase completion.
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_u32(b)) : "memory");
+}
+// Arrive once every cp.async copy issued so far by this thread has landed.
+__device__ __forceinline__ void cp_async_mbar_arrive(unsigned long long* b) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Warp-uniform wait for the completion of phase `parity` of mbarrier b.
+// Returns false, for the whole warp, after about 2^31 cycles (a second).
+__device__ __forceinline__ bool warp_wait(unsigned long long* b, unsigned parity) {
+  bool done = mbar_try_wait(b, parity);
+  if (__all_sync(kFull, done)) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    done = done || mbar_try_wait(b, parity);
+    if (__all_sync(kFull, done)) return true;
+    const int late = (clock64() - t0) > (1LL << 31) ? 1 : 0;
+    if (__shfl_sync(kFull, late, 0)) return false;
+  }
+}
+
 inline int launch_status() {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CPIC_OK : CPIC_ECUDA;

@@ -22,22 +22,23 @@
 //   cell order: a 13-shuffle reduce-scatter leaves 12 totals for 12 lanes,
 //   one atomic each), the other lanes use 16-byte vector reductions
 //   (red.global.add.v4.f32).
-//   push_tiled_kernel (default).  A CTA takes tiles of
-//   32 * 8 * chunks_per_warp consecutive particles.  Once particles are in cell
-//   order a tile covers a short run of voxels [lo, hi]; its cell window is that
-//   run widened by one voxel on each side (the segment [c0, c0 + wx)) together
-//   with the eight segments offset by +-1 in y and z (strides sx, sx*sy): 9
-//   segments, every cell a particle of the tile reaches some steps after a
-//   sort.  The 18 interpolator coefficients of the window's cells are staged in
-//   shared memory (rows of 20 values, 16-byte aligned) by cp.async copies
-//   issued one tile ahead (two buffers), so a gather is five vector shared
-//   loads instead of 18 dependent global loads.  A particle whose cell has no
-//   slot gathers from global memory, so results do not depend on the order,
-//   only the speed does.  The window is anchored on the median of 32 sampled
-//   cells of the tile, computed by warp 0 two tiles ahead.  Deposits as in
-//   push_kernel.  (A shared accumulator window was measured slower: shared
-//   float atomics are compare-and-swap loops, and the global reductions of
-//   reduced groups are cheap.)
+//   push_tiled_kernel (default).  A CTA takes tiles of 32 * 7 * chunks_per_warp
+//   consecutive particles.  Once particles are in cell order a tile covers a
+//   short run of voxels [lo, hi]; its cell window is that run widened by one
+//   voxel on each side (the segment [c0, c0 + wx)) together with the eight
+//   segments offset by +-1 in y and z (strides sx, sx*sy): 9 segments, every
+//   cell a particle of the tile reaches some steps after a sort.  Warp 0 is a
+//   producer: it anchors each tile's window on the median of 32 sampled cells
+//   and stages the 18 interpolator coefficients of the window's cells in
+//   shared memory (rows of 20 values, 16-byte aligned) with cp.async, into two
+//   buffers handed over through mbarriers.  Warps 1..7 push the particles: a
+//   gather is five vector shared loads instead of 18 dependent global loads; a
+//   particle whose cell has no slot gathers from global memory, so results do
+//   not depend on the order, only the speed does.  Deposits as in
+//   push_kernel.  (Measured and dropped: a shared accumulator window, since
+//   shared float atomics are compare-and-swap loops and the global reductions
+//   of reduced groups are cheap; and a CTA-wide barrier per tile in place of
+//   the producer warp, which cost a fifth of the warps' time in barrier stalls.)
 //
 // In both, cell-crossing particles are compacted into a per-warp shared-memory
 // queue (ballot + prefix popcount) holding the particle index and its
@@ -81,7 +82,10 @@ constexpr int kRow = 20;         // window row: 18 coefficients + 2 pad
 
 template <class R>
 struct MoverQueue {
+  R px[kQueueCap], py[kQueueCap], pz[kQueueCap];  // offsets before the move
   R dx[kQueueCap], dy[kQueueCap], dz[kQueueCap];  // normalised half displacement
+  R q[kQueueCap];
+  int cell[kQueueCap];
   int idx[kQueueCap];
 };
 
@@ -209,19 +213,13 @@ __device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool
   }
 }
 
-// move_p for one particle (src/move_p.h:93-371): reads the particle's offsets,
-// weight and cell (unchanged in memory for a crosser), runs the streaks with
-// the half displacement (dx, dy, dz) and writes the final offsets and cell.
+// move_p for one particle (src/move_p.h:93-371), positions and displacement in
+// registers; writes the final offsets and cell of particle `pidx`.
 template <class R, int VL>
-__device__ __noinline__ void move_one(unsigned char* __restrict__ part, R dx, R dy, R dz, int pidx,
-                                      R qsp, R* __restrict__ acc, const GridDev g,
-                                      int* __restrict__ status) {
+__device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R py, R pz, R dx,
+                                      R dy, R dz, R q, int cell, int pidx, R* __restrict__ acc,
+                                      const GridDev g, int* __restrict__ status) {
   using L = PLayout<R, VL>;
-  R px = *reinterpret_cast<const R*>(part + L::off(pidx, 0));
-  R py = *reinterpret_cast<const R*>(part + L::off(pidx, 1));
-  R pz = *reinterpret_cast<const R*>(part + L::off(pidx, 2));
-  const R q = *reinterpret_cast<const R*>(part + L::off(pidx, 6)) * qsp;
-  int cell = *reinterpret_cast<const int*>(part + L::cell_off(pidx));
   if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) atomicOr(status, CPIC_STATUS_NONFINITE);
   bool done = false;
   for (int it = 0; it < kMaxStreaks; ++it) {
@@ -471,18 +469,20 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
   if (cm) {
     if (cross) {
       const int s = qn + __popc(cm & lc.lt_mask);
+      Q.px[s] = x; Q.py[s] = y; Q.pz[s] = z;
       Q.dx[s] = ux; Q.dy[s] = uy; Q.dz[s] = uz;
-      Q.idx[s] = p;
+      Q.q[s] = q; Q.cell[s] = cell; Q.idx[s] = p;
     }
     qn += __popc(cm);
     if (qn >= 32) {
       __syncwarp();
       const int s = qn - 32 + lc.lane;
-      const R ddx = Q.dx[s], ddy = Q.dy[s], ddz = Q.dz[s];
-      const int ii = Q.idx[s];
+      const R ex0 = Q.px[s], ey0 = Q.py[s], ez0 = Q.pz[s];
+      const R ddx = Q.dx[s], ddy = Q.dy[s], ddz = Q.dz[s], qq = Q.q[s];
+      const int cc = Q.cell[s], ii = Q.idx[s];
       __syncwarp();
       qn -= 32;
-      move_one<R, VL>(part, ddx, ddy, ddz, ii, a.qsp, acc, a.g, status);
+      move_one<R, VL>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, status);
     }
   }
 }
@@ -505,7 +505,9 @@ __device__ __forceinline__ void drain_queue(unsigned char* __restrict__ part, Mo
                                             int lane, const PushArgs<R>& a, R* __restrict__ acc,
                                             int* __restrict__ status) {
   __syncwarp();
-  if (lane < qn) move_one<R, VL>(part, Q.dx[lane], Q.dy[lane], Q.dz[lane], Q.idx[lane], a.qsp, acc, a.g, status);
+  if (lane < qn)
+    move_one<R, VL>(part, Q.px[lane], Q.py[lane], Q.pz[lane], Q.dx[lane], Q.dy[lane], Q.dz[lane],
+                    Q.q[lane], Q.cell[lane], Q.idx[lane], acc, a.g, status);
 }
 
 // ------------------------------------------------------------ streaming kernel
@@ -606,14 +608,14 @@ __device__ __forceinline__ int slot_segment(int i, float inv_wx) {
   return min((int)(((float)i + 0.5f) * inv_wx), 8);
 }
 
-// Issues the copies of the window's interpolator rows (one thread per window
+// Issues the copies of the window's interpolator rows (one lane per window
 // cell, 18 asynchronous element copies); cells outside the array read as 0.
 template <class R>
 __device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __restrict__ interp,
-                                             const TileWin w, int ys, int zs, int num_cells) {
+                                             const TileWin w, int ys, int zs, int num_cells, int lane) {
   const int ncell = 9 * w.wx;
   const float inv_wx = 1.0f / (float)w.wx;
-  for (int i = threadIdx.x; i < ncell; i += kPushThreads) {
+  for (int i = lane; i < ncell; i += 32) {
     const int s = slot_segment(i, inv_wx);
     const int gc = segment_start(w, s, ys, zs) + (i - s * w.wx);
     R* row = buf + i * kRow;
@@ -630,6 +632,8 @@ __device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __res
 
 // Shared memory of the tiled kernel beyond its static part: two interpolator
 // windows of 9 * wxmax cells.
+constexpr int kConsumers = kWarps - 1;  // warps 1..7 push; warp 0 stages windows
+
 template <class R>
 constexpr size_t tiled_dyn_smem(int wxmax) {
   return (size_t)9 * wxmax * 2 * kRow * sizeof(R);
@@ -645,70 +649,90 @@ __device__ __forceinline__ int tile_sample(const unsigned char* __restrict__ par
   return __ldcg(reinterpret_cast<const int*>(part + L::cell_off(p)));
 }
 
+// Warp 0 produces: for tile j it waits until the consumers have released
+// buffer j % 2 (used by tile j - 2), computes the window from the samples,
+// publishes it and stages the rows with cp.async; each lane arrives on
+// full[j % 2] twice, once when its copies land and once (release) after its
+// plain shared stores.  Warps 1..7 consume: they wait for full[j % 2], push
+// their chunks of tile j gathering from the window, and arrive on
+// empty[j % 2].  No CTA-wide barrier: a warp delayed by a queue drain holds up
+// nobody until the producer needs its buffer again.
 template <class R, int VL, bool LITERAL, bool FAST>
-__global__ void __launch_bounds__(kPushThreads)
+__global__ void __launch_bounds__(kPushThreads, sizeof(R) == 4 ? 4 : 2)  // FP32: 64 registers
 push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
                   R* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status,
                   int chunks_per_warp, int wxmax) {
   constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R* const wbuf0 = reinterpret_cast<R*>(smem_raw);
-  R* const wbuf1 = wbuf0 + 9 * wxmax * kRow;
-  __shared__ MoverQueue<R> queues[kWarps];
-  __shared__ TileWin wins[3];
+  R* const wbuf = reinterpret_cast<R*>(smem_raw);  // two windows of 9 * wxmax rows
+  __shared__ MoverQueue<R> queues[kConsumers];
+  __shared__ TileWin wins[2];
+  __shared__ __align__(8) unsigned long long full[2], empty[2];
   const int warp = threadIdx.x >> 5;
-  MoverQueue<R>& Q = queues[warp];
   const LaneCtx lc = make_lane_ctx<R, VL>();
-  const int cpt = kWarps * chunks_per_warp;  // chunks per tile
-  const int T = 32 * cpt;                    // particles per tile
+  const int cpt = kConsumers * chunks_per_warp;  // chunks per tile
+  const int T = 32 * cpt;                        // particles per tile
   const int ntiles = (int)(((int64_t)n + T - 1) / T);
   const int nchunks = (n + 31) >> 5;
   const int ys = a.g.sx, zs = a.g.sx * a.g.sy, nc = a.g.num_cells;
   const int G = gridDim.x;
-  int t = blockIdx.x;
-  if (t >= ntiles) return;
-
-  // prologue: warp 0 sets the windows of the first two tiles and loads the
-  // samples of the third
-  int sample = 0;
-  if (warp == 0) {
-    TileWin w0 = window_from_samples(tile_sample<R, VL>(part, n, T, t, lc.lane), lc.lane, wxmax, nc);
-    TileWin w1 = w0;
-    if (t + G < ntiles)
-      w1 = window_from_samples(tile_sample<R, VL>(part, n, T, t + G, lc.lane), lc.lane, wxmax, nc);
-    if (lc.lane == 0) { wins[0] = w0; wins[1] = w1; }
-    if (t + 2 * G < ntiles) sample = tile_sample<R, VL>(part, n, T, t + 2 * G, lc.lane);
+  const size_t wrows = (size_t)9 * wxmax * kRow;
+  if ((int)blockIdx.x >= ntiles) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&full[0], 64);
+    mbar_init(&full[1], 64);
+    mbar_init(&empty[0], kConsumers);
+    mbar_init(&empty[1], kConsumers);
   }
   __syncthreads();
-  stage_window<R>(wbuf0, interp, wins[0], ys, zs, nc);
-  cp_async_commit();
 
+  if (warp == 0) {  // ---------------------------------------- producer
+    int s_cur = tile_sample<R, VL>(part, n, T, blockIdx.x, lc.lane);
+    int s_nxt = (int)blockIdx.x + G < ntiles ? tile_sample<R, VL>(part, n, T, blockIdx.x + G, lc.lane) : 0;
+    bool ok = true;
+    int j = 0;
+    for (int t = blockIdx.x; t < ntiles; t += G, ++j) {
+      const int b = j & 1;
+      if (j >= 2 && !warp_wait(&empty[b], (unsigned)((j >> 1) - 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      const TileWin w = window_from_samples(s_cur, lc.lane, wxmax, nc);
+      s_cur = s_nxt;
+      if (t + 2 * G < ntiles) s_nxt = tile_sample<R, VL>(part, n, T, t + 2 * G, lc.lane);
+      if (lc.lane == 0) wins[b] = w;
+      stage_window<R>(wbuf + b * wrows, interp, w, ys, zs, nc, lc.lane);
+      cp_async_mbar_arrive(&full[b]);
+      mbar_arrive(&full[b]);
+    }
+    cp_async_wait_all();
+    if (!ok && lc.lane == 0) atomicOr(status, CPIC_STATUS_PIPELINE);
+    return;
+  }
+
+  // ---------------------------------------------------------- consumers
+  const int cw = warp - 1;
+  MoverQueue<R>& Q = queues[cw];
   int qn = 0;
-  int chunk = t * cpt + warp;
+  int t = blockIdx.x;
+  int chunk = t * cpt + cw;
   PState<R> cur;
   load_state<R, VL>(part + (size_t)chunk * kChunk, lc.lane_off, lc.lane_cell_off,
                     chunk < nchunks && chunk * 32 + lc.lane < n, cur);
+  bool ok = true;
   for (int j = 0; t < ntiles; ++j, t += G) {
-    cp_async_wait_all();
-    // window j staged by every thread; window j+1 published; every warp done
-    // reading the buffer that window j+1 is staged into
-    __syncthreads();
-    const TileWin w = wins[j % 3];
-    const R* const wb = (j & 1) ? wbuf1 : wbuf0;
+    const int b = j & 1;
+    if (!warp_wait(&full[b], (unsigned)(j >> 1) & 1u)) {
+      ok = false;
+      break;
+    }
+    const TileWin w = wins[b];
+    const R* const wb = wbuf + b * wrows;
     const int t1 = t + G;
-    if (t1 < ntiles) {
-      stage_window<R>((j & 1) ? wbuf0 : wbuf1, interp, wins[(j + 1) % 3], ys, zs, nc);
-      cp_async_commit();
-    }
-    if (warp == 0 && t1 + G < ntiles) {
-      const TileWin w2 = window_from_samples(sample, lc.lane, wxmax, nc);
-      if (lc.lane == 0) wins[(j + 2) % 3] = w2;
-      if (t1 + 2 * G < ntiles) sample = tile_sample<R, VL>(part, n, T, t1 + 2 * G, lc.lane);
-    }
     for (int i = 0; i < chunks_per_warp; ++i) {
-      chunk = t * cpt + warp + kWarps * i;
+      chunk = t * cpt + cw + kConsumers * i;
       const bool last = i + 1 == chunks_per_warp;
-      const int next = last ? t1 * cpt + warp : chunk + kWarps;
+      const int next = last ? t1 * cpt + cw : chunk + kConsumers;
       PState<R> nxt;
       load_state<R, VL>(part + (size_t)next * kChunk, lc.lane_off, lc.lane_cell_off,
                         (!last || t1 < ntiles) && next < nchunks && next * 32 + lc.lane < n, nxt);
@@ -717,7 +741,10 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
                                                lc, wb, w, ys, zs);
       cur = nxt;
     }
+    __syncwarp();
+    if (lc.lane == 0) mbar_arrive(&empty[b]);
   }
+  if (!ok && lc.lane == 0) atomicOr(status, CPIC_STATUS_PIPELINE);
   drain_queue<R, VL>(part, Q, qn, lc.lane, a, acc, status);
 }
 
@@ -756,7 +783,7 @@ inline TileShape tile_shape(int64_t n, const GridDev& g) {
   const double ppc = (double)n / ((double)g.nx * g.ny * g.nz);
   TileShape ts{1, 32};
   for (int cpw = 4; cpw >= 1; --cpw) {
-    const double cells = 32.0 * kWarps * cpw / (ppc > 1e-9 ? ppc : 1e-9);
+    const double cells = 32.0 * kConsumers * cpw / (ppc > 1e-9 ? ppc : 1e-9);
     const int wx = (int)(1.25 * cells) + 4;  // slack for cell-count fluctuations
     if (wx <= 32 || cpw == 1) {
       ts.chunks_per_warp = cpw;
@@ -792,7 +819,7 @@ int launch_push_tiled(void* particles, int n, const void* interp, void* acc, con
     occ_blocks[dev] = b;
     occ_dyn[dev] = dyn;
   }
-  const int64_t T = 32LL * kWarps * ts.chunks_per_warp;
+  const int64_t T = 32LL * kConsumers * ts.chunks_per_warp;
   const int64_t ntiles = ((int64_t)n + T - 1) / T;
   int64_t blocks = (int64_t)sm_count() * occ_blocks[dev];
   if (blocks > ntiles) blocks = ntiles;

@@ -42,6 +42,8 @@ typedef struct CUstream_st* cpic_stream_t;
 #define CPIC_STATUS_CELL_RANGE 1  /* particle cell index outside [0, num_cells): skipped */
 #define CPIC_STATUS_MOVER_CAP 2   /* move_p streak loop hit its iteration cap */
 #define CPIC_STATUS_NONFINITE 4   /* non-finite displacement met in move_p */
+#define CPIC_STATUS_PIPELINE 8    /* a bounded wait inside the tiled push kernel gave up
+                                     (about a second); the push is incomplete */
 
 /* Boundary, src/input/deck.h:9-12 */
 #define CPIC_REFLECT 0
