@@ -608,30 +608,32 @@ __device__ __forceinline__ int slot_segment(int i, float inv_wx) {
   return min((int)(((float)i + 0.5f) * inv_wx), 8);
 }
 
-// Issues the copies of the window's interpolator rows (one lane per window
-// cell, 18 asynchronous element copies); cells outside the array read as 0.
+// Issues the copies of the window's interpolator rows; cells outside the
+// array read as 0.  One copy instruction covers 8 cells x 4 members: lane l
+// takes slot 8g + l / 4 and members l % 4, l % 4 + 4, ...  Rows are 20 words,
+// so the 8 slots start in 8 distinct banks (20 * slot mod 32) and the 4
+// members fill the banks between: each copy writes 32 distinct banks.
 template <class R>
 __device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __restrict__ interp,
                                              const TileWin w, int ys, int zs, int num_cells, int lane) {
   const int ncell = 9 * w.wx;
   const float inv_wx = 1.0f / (float)w.wx;
-  for (int i = lane; i < ncell; i += 32) {
+  const int q = lane & 3;
+  for (int i = lane >> 2; i < ncell; i += 8) {
     const int s = slot_segment(i, inv_wx);
     const int gc = segment_start(w, s, ys, zs) + (i - s * w.wx);
     R* row = buf + i * kRow;
     if ((unsigned)gc < (unsigned)num_cells) {
       const R* src = interp + ((size_t)(gc >> 5) * (18 * kCellBlock) + (gc & 31));
 #pragma unroll
-      for (int m = 0; m < 18; ++m) cp_async_elem<R>(row + m, src + m * kCellBlock);
+      for (int m = q; m < 18; m += 4) cp_async_elem<R>(row + m, src + m * kCellBlock);
     } else {
 #pragma unroll
-      for (int m = 0; m < 18; ++m) row[m] = R(0);
+      for (int m = q; m < 18; m += 4) row[m] = R(0);
     }
   }
 }
 
-// Shared memory of the tiled kernel beyond its static part: two interpolator
-// windows of 9 * wxmax cells.
 constexpr int kConsumers = kWarps - 1;  // warps 1..7 push; warp 0 stages windows
 
 template <class R>
