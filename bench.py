@@ -39,6 +39,7 @@ SORT_INTERVAL = 20
 N_CELLS = 128
 PPC = 64
 TILES = True
+WORKLOAD = "thermal"
 # algorithmic bytes of push+deposit: per particle read 7 reals + cell, write 6
 # reals; per interior cell the 18 interpolator coefficients and 12 accumulators
 BYTES_PER_PARTICLE = {4: 56, 8: 108}
@@ -151,17 +152,27 @@ def _barrier(ws):
 
 
 # ---------------------------------------------------------------- GPU arm
+def _deck(precision, steps):
+    from cabanapic_gb300 import decks
+    if WORKLOAD == "diocotron":
+        return decks.diocotron(precision=precision, num_steps=steps)
+    return decks.thermal(n=N_CELLS, ppc=PPC, precision=precision, num_steps=steps)
+
+
 def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     """Device-resident timed loop; returns dict with times and push events."""
     import torch
     from cabanapic_gb300 import decks
     from cabanapic_gb300.simulation import Simulation
 
-    deck = decks.thermal(n=N_CELLS, ppc=PPC, precision=precision, num_steps=steps + warmup)
-    if host_packed is None:
+    deck = _deck(precision, steps + warmup)
+    fields = None
+    if WORKLOAD == "diocotron":
+        host_packed, fields = decks.diocotron_state(deck, packed=True)
+    elif host_packed is None:
         host_packed = decks.thermal_particles(deck, packed=True)
     sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup,
-                     exact=exact, tiles=TILES)
+                     exact=exact, tiles=TILES, fields=fields)
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
         sim.step()
@@ -272,7 +283,7 @@ def cpu_sample_run(steps, warmup, precision=4, sample_ppc=8, threads=0):
 
 # ---------------------------------------------------------------- main
 def main():
-    global N_CELLS, PPC, TILES
+    global N_CELLS, PPC, TILES, WORKLOAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -284,10 +295,14 @@ def main():
     ap.add_argument("--no-exact", action="store_true")
     ap.add_argument("--cells", type=int, default=N_CELLS, help="cells per axis (profiling cases)")
     ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (profiling cases)")
+    ap.add_argument("--workload", default="thermal", choices=["thermal", "diocotron"],
+                    help="thermal: the headline 128^3 x 64 ppc plasma; diocotron: the 96x96x64 "
+                         "column at 128 ppc (heavy cell crossing), push + step timing only")
     ap.add_argument("--streaming", action="store_true",
                     help="streaming push kernel instead of the tiled one (comparison runs)")
     args = ap.parse_args()
     N_CELLS, PPC, TILES = args.cells, args.ppc, not args.streaming
+    WORKLOAD = args.workload
     ws, rank, local = _dist()
     metric = "particle-pushes/s (full step, FP32)"
     unit = "particle-pushes/s"
@@ -333,6 +348,23 @@ def main():
     alg_bytes = n * BYTES_PER_PARTICLE[4] + deck.num_interior * BYTES_PER_CELL[4]
     peak, peak_kind = _peaks()
     achieved = alg_bytes / (push_ms / 1e3) / 1e9
+    if WORKLOAD == "diocotron":
+        if rank == 0:
+            print(json.dumps({
+                "metric": metric, "value": value, "unit": unit, "n_gpus": ws, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "diocotron column 96x96x64 cells, annulus 0.20<r/R<0.35 at 128 "
+                                       "particles per cell of annulus volume, cB_z = 5, E x B loading "
+                                       "from the t=0 Poisson field, dt=0.99 Courant, sort every 20 steps",
+                           "particles": n, "cells": deck.num_cells,
+                           "push_kernel": "tiled" if TILES else "streaming"},
+                "push_ms": push_ms, "push_ms_by_step": [round(t, 4) for t in res["push_ms"]],
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind,
+                             "algorithmic_bytes_per_launch": alg_bytes},
+                "clocks": clocks}), flush=True)
+        return
     traffic = _traffic_from_profiles()
     per_step_launches = 11  # interp, push, unload, 2x(advance_b + ghost copy), fold, ghost copy, advance_e, energies
     launches = args.steps * per_step_launches + 6 * len(range(0, args.steps, SORT_INTERVAL))

@@ -774,25 +774,22 @@ int launch_push(void* particles, int n, const void* interp, void* acc, const Pus
   return launch_status();
 }
 
-// Tile shape from the mean particles per interior cell: the largest tile
-// (up to 4 chunks per warp, 1024 particles) whose sorted run of cells, with
-// one voxel of margin each side, fits a window of at most 32 voxels.
+// Tile shape: 4 chunks per consumer warp (896 particles).  Each tile sizes its
+// own window from its sampled cells (a run of 896 / ppc voxels plus margins),
+// so the shape does not depend on the mean particle density, which says little
+// when particles fill part of the box; wxmax only bounds the shared memory.
+// Two windows of 9 x 21 rows take 30.2 KB in FP32, 46.4 KB per CTA with the
+// mover queues: four CTAs fit the 196 KB shared-memory carveout and leave
+// 60 KB of L1 (24 rows tip them into the 228 KB carveout, 28 KB of L1, and
+// the push was measured 9% slower).  Runs longer than wxmax - 2 voxels (under
+// ~47 particles per cell) get a window centred on the median sample and the
+// rest of the tile gathers from global memory.
 struct TileShape {
   int chunks_per_warp, wxmax;
 };
 
-inline TileShape tile_shape(int64_t n, const GridDev& g) {
-  const double ppc = (double)n / ((double)g.nx * g.ny * g.nz);
-  TileShape ts{1, 32};
-  for (int cpw = 4; cpw >= 1; --cpw) {
-    const double cells = 32.0 * kConsumers * cpw / (ppc > 1e-9 ? ppc : 1e-9);
-    const int wx = (int)(1.25 * cells) + 4;  // slack for cell-count fluctuations
-    if (wx <= 32 || cpw == 1) {
-      ts.chunks_per_warp = cpw;
-      ts.wxmax = wx < 32 ? wx : 32;
-      break;
-    }
-  }
+inline TileShape tile_shape(const GridDev& g) {
+  TileShape ts{4, 21};
   if (ts.wxmax > g.sx) ts.wxmax = g.sx;  // segments of one window must not overlap
   if (ts.wxmax < 3) ts.wxmax = 3;
   return ts;
@@ -802,7 +799,7 @@ template <class R, int VL, bool LITERAL, bool FAST>
 int launch_push_tiled(void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
                       int* status, cudaStream_t s) {
   auto kern = push_tiled_kernel<R, VL, LITERAL, FAST>;
-  const TileShape ts = tile_shape(n, a.g);
+  const TileShape ts = tile_shape(a.g);
   const size_t dyn = tiled_dyn_smem<R>(ts.wxmax);
   static size_t opted[64] = {0};
   static size_t occ_dyn[64] = {0};

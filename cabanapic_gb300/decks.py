@@ -11,6 +11,11 @@ Initializers:
                      (src/input/deck.h:79-158), used by its 2stream-em test deck
   two_stream_1d      seeded two-beam plasma along x with a sin(kx) perturbation
   thermal            seeded uniform Maxwellian plasma, particles in cell order
+  diocotron          3-D electron column (annulus) in a uniform axial B, loaded
+                     at the local E x B drift of its own field, which is solved
+                     on the grid at t = 0 (discrete Poisson equation, FFT)
+  diocotron_slab     the reference's decks/dioctron_3d.cxx: a y-strip of cold
+                     electrons in a uniform B_z with a sheared E_y field
 """
 from __future__ import annotations
 
@@ -47,6 +52,7 @@ class Deck:
     vl: int = 32                # particle AoSoA vector length
     name: str = "deck"
     extra: dict = field(default_factory=dict)
+    n_particles: int = 0        # particle count when not nppc per interior cell
 
     @property
     def R(self):
@@ -63,6 +69,8 @@ class Deck:
 
     @property
     def num_particles(self) -> int:
+        if self.n_particles > 0:
+            return self.n_particles
         return self.nx * self.ny * self.nz * self.nppc
 
     def derived(self) -> dict:
@@ -234,9 +242,208 @@ def thermal_particles(deck: Deck, packed: bool = False, n_sample: int = None):
     return out
 
 
+# ---------------------------------------------------------------- diocotron
+def diocotron(precision: int = 4, vl: int = 32, n=(96, 96, 64), ppc: int = 128, dx: float = 0.2,
+              b0: float = 5.0, r_in: float = 0.20, r_out: float = 0.35, amp: float = 0.01,
+              mode: int = 3, num_steps: int = 2000, seed: int = 7) -> Deck:
+    """3-D diocotron column on an n = (nx, ny, nz) periodic grid of cubic cells
+    of size dx (c / w_pe units, c = eps0 = m_e = |q| = 1): uniform axial field
+    cB_z = b0 (w_ce / w_pe = b0 at the column's density 1), electrons only in
+    the annulus r_in < r / R < r_out around the box axis (R = half the
+    transverse width) at ppc particles per cell of annulus volume, an azimuthal
+    density perturbation 1 + amp cos(mode theta) carried by the weights, cold
+    momenta at the local E x B drift, a uniform neutralising background,
+    dt = 0.99 x the Courant limit (as decks/dioctron_3d.cxx)."""
+    R = np.float32 if precision == 4 else np.float64
+    nx, ny, nz = (int(v) for v in n)
+    lx, ly, lz = nx * dx, ny * dx, nz * dx
+    rad = 0.5 * min(lx, ly)
+    area_cells = math.pi * (r_out ** 2 - r_in ** 2) * rad * rad / (dx * dx)
+    npart = int(round(ppc * area_cells * nz))
+    npart -= npart % 32 if npart > 64 else 0
+    d = Deck(nx=nx, ny=ny, nz=nz, nppc=ppc, num_steps=num_steps, v0=0.0,
+             len_x_global=lx, len_y_global=ly, len_z_global=lz, n0=1.0, precision=precision,
+             vl=vl, name="diocotron", n_particles=npart,
+             extra=dict(b0=b0, r_in=r_in, r_out=r_out, amp=amp, mode=mode, seed=seed, radius=rad))
+    d.dt = float(R(0.99 * f64(courant_length(lx, ly, lz, nx, ny, nz, R))))
+    return d
+
+
+def node_charge_density(p: dict, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
+                        qsp: float) -> np.ndarray:
+    """Charge density at the nodes (low corners of the voxels), FP64, as
+    (nz, ny, nx) over the interior nodes: trilinear weights of each particle
+    to the 8 corners of its voxel, the n + 1 layer folded onto node 1
+    (periodic)."""
+    sx, sy = nx + 2, ny + 2
+    c = p["cell"].astype(np.int64)
+    iy, ix = np.divmod(c, sx)
+    iz, iy = np.divmod(iy, sy)
+    x, y, z = (p[k].astype(np.float64) for k in ("x", "y", "z"))
+    q = p["w"].astype(np.float64) * (qsp / (dx * dy * dz))
+    rho = np.zeros((nz, ny, nx))
+    wx = (0.5 * (1 - x), 0.5 * (1 + x))
+    wy = (0.5 * (1 - y), 0.5 * (1 + y))
+    wz = (0.5 * (1 - z), 0.5 * (1 + z))
+    for a in (0, 1):
+        jx = (ix - 1 + a) % nx
+        for b in (0, 1):
+            jy = (iy - 1 + b) % ny
+            for e in (0, 1):
+                jz = (iz - 1 + e) % nz
+                np.add.at(rho, (jz, jy, jx), q * wx[a] * wy[b] * wz[e])
+    return rho
+
+
+def poisson_edge_fields(rho: np.ndarray, dx: float, dy: float, dz: float, eps0: float = 1.0):
+    """E = -grad(phi) on the Yee edges for node charge rho (nz, ny, nx) plus a
+    uniform neutralising background: the discrete Poisson equation whose
+    divergence is the backward-difference div E at the nodes, solved exactly
+    by FFT on the periodic grid.  Returns (ex, ey, ez), each (nz, ny, nx):
+    ex[k, j, i] on the edge from node i to node i + 1."""
+    nz, ny, nx = rho.shape
+    r = rho - rho.mean()
+    kx = 2 - 2 * np.cos(2 * np.pi * np.arange(nx) / nx)
+    ky = 2 - 2 * np.cos(2 * np.pi * np.arange(ny) / ny)
+    kz = 2 - 2 * np.cos(2 * np.pi * np.arange(nz) / nz)
+    lap = (kz[:, None, None] / (dz * dz) + ky[None, :, None] / (dy * dy)
+           + kx[None, None, :] / (dx * dx))
+    lap[0, 0, 0] = 1.0
+    ph = np.fft.fftn(r / eps0) / lap
+    ph[0, 0, 0] = 0.0
+    phi = np.real(np.fft.ifftn(ph))
+    ex = -(np.roll(phi, -1, axis=2) - phi) / dx
+    ey = -(np.roll(phi, -1, axis=1) - phi) / dy
+    ez = -(np.roll(phi, -1, axis=0) - phi) / dz
+    return ex, ey, ez
+
+
+def _edge_fields_to_cells(deck: Deck, ex, ey, ez, cbz: float) -> np.ndarray:
+    """(num_cells, 9) field members: E edges of interior voxel (i, j, k) from the
+    (nz, ny, nx) arrays, periodic images in the ghost layers, uniform cB_z."""
+    nx, ny, nz = deck.nx, deck.ny, deck.nz
+    F = np.zeros((nz + 2, ny + 2, nx + 2, 9))
+    for m, e in enumerate((ex, ey, ez)):
+        F[..., m] = np.pad(e, 1, mode="wrap")
+    F[..., 5] = cbz
+    return F.reshape(-1, 9).astype(deck.R)
+
+
+def diocotron_state(deck: Deck, packed: bool = False):
+    """(particles, fields) at t = 0 for the diocotron deck; particles in cell
+    order, fields as (num_cells, 9) member values."""
+    R = deck.R
+    ex_ = deck.extra
+    rng = np.random.default_rng(ex_.get("seed", 7))
+    n = deck.num_particles
+    p = deck.derived()
+    dx, dy, dz = (float(p[k]) for k in ("dx", "dy", "dz"))
+    lx, ly, lz = deck.len_x_global, deck.len_y_global, deck.len_z_global
+    rad = ex_["radius"]
+    r = np.sqrt(rng.uniform((ex_["r_in"] * rad) ** 2, (ex_["r_out"] * rad) ** 2, n))
+    th = rng.uniform(0.0, 2 * np.pi, n)
+    X = 0.5 * lx + r * np.cos(th)
+    Y = 0.5 * ly + r * np.sin(th)
+    Z = rng.uniform(0.0, lz, n)
+    gx, gy, gz = X / dx, Y / dy, Z / dz
+    ix = np.minimum(np.floor(gx).astype(np.int64), deck.nx - 1)
+    iy = np.minimum(np.floor(gy).astype(np.int64), deck.ny - 1)
+    iz = np.minimum(np.floor(gz).astype(np.int64), deck.nz - 1)
+    ox, oy, oz = 2 * (gx - ix) - 1, 2 * (gy - iy) - 1, 2 * (gz - iz) - 1
+    vol = math.pi * (ex_["r_out"] ** 2 - ex_["r_in"] ** 2) * rad * rad * lz
+    w = (deck.n0 * vol / n) * (1 + ex_["amp"] * np.cos(ex_["mode"] * th))
+    cell = L.voxel(ix + 1, iy + 1, iz + 1, deck.nx, deck.ny).astype(np.int32)
+    part = dict(x=ox.astype(R), y=oy.astype(R), z=oz.astype(R), w=w.astype(R), cell=cell)
+    # the column's field (and the background's) on the grid, then the drift
+    rho = node_charge_density(part, deck.nx, deck.ny, deck.nz, dx, dy, dz, float(p["qsp"]))
+    exg, eyg, ezg = poisson_edge_fields(rho, dx, dy, dz, float(p["eps"]))
+    fx = 0.5 * (1 - part["x"].astype(f64))
+    fy = 0.5 * (1 - part["y"].astype(f64))
+    jx, jy, jz = ix, iy, iz
+    # edge values bilinear across the voxel (the push's interpolation for z-uniform fields)
+    Ex = (fy * exg[jz, jy, jx] + (1 - fy) * exg[jz, (jy + 1) % deck.ny, jx])
+    Ey = (fx * eyg[jz, jy, jx] + (1 - fx) * eyg[jz, jy, (jx + 1) % deck.nx])
+    b0 = ex_["b0"]
+    vx, vy = Ey / b0, -Ex / b0
+    gam = 1.0 / np.sqrt(1.0 - np.minimum(vx * vx + vy * vy, 0.99))
+    part.update(ux=(gam * vx).astype(R), uy=(gam * vy).astype(R), uz=np.zeros(n, R))
+    order = np.argsort(cell, kind="stable")
+    part = {k: v[order] for k, v in part.items()}
+    fields = _edge_fields_to_cells(deck, exg, eyg, ezg, b0)
+    if packed:
+        part = L.pack_particles(part, R, deck.vl)
+    return part, fields
+
+
+def diocotron_slab(precision: int = 4, vl: int = 32, num_steps: int = 20000, seed: int = 5) -> Deck:
+    """decks/dioctron_3d.cxx: 64 x 64 x 1 cells, Lx = Ly = 16 a (a = 0.1),
+    Lz = 1, 5 particles per cell of the box, dt = 0.99 Courant, v0 = 0."""
+    R = np.float32 if precision == 4 else np.float64
+    a = 0.1
+    d = Deck(nx=64, ny=64, nz=1, nppc=5, num_steps=num_steps, v0=0.0, len_x_global=16 * a,
+             len_y_global=16 * a, len_z_global=1.0, n0=1.0, precision=precision, vl=vl,
+             name="diocotron-slab", extra=dict(a=a, seed=seed))
+    d.dt = float(R(R(0.99) * courant_length(d.len_x_global, d.len_y_global, d.len_z_global, 64, 64, 1, R)))
+    return d
+
+
+def diocotron_slab_state(deck: Deck, packed: bool = False):
+    """Custom_Particle_Initializer and Custom_Field_Initializer of
+    decks/dioctron_3d.cxx:4-165: particles uniform in x over the box and in
+    |y| < a, z offset 0 in the first z layer, at rest, weight we; fields
+    cB_z = sqrt(20) and E_y = a for y < -a, -a for y > a, -y between, with
+    y = ymin + (iy - 0.5) dy.  The reference draws positions with rand(); a
+    seeded generator stands in."""
+    R = deck.R
+    p = deck.derived()
+    a = deck.extra["a"]
+    rng = np.random.default_rng(deck.extra.get("seed", 5))
+    n = deck.num_particles
+    nx, ny, nz = deck.nx, deck.ny, deck.nz
+    lx, ly = deck.len_x_global, deck.len_y_global
+    hx, hy = lx / nx, ly / ny
+    xmin, ymin = -0.5 * lx, -0.5 * ly
+    gx = (rng.uniform(-0.5 * lx, 0.5 * lx, n) - xmin) / hx
+    ix = gx.astype(np.int64)
+    ox = 2 * (gx - ix) - 1
+    ox = np.where(ix == nx, 1.0, ox); ix = np.where(ix == nx, nx - 1, ix)
+    gy = (rng.uniform(-a, a, n) - ymin) / hy
+    iy = gy.astype(np.int64)
+    oy = 2 * (gy - iy) - 1
+    oy = np.where(iy == ny, 1.0, oy); iy = np.where(iy == ny, ny - 1, iy)
+    cell = L.voxel(ix + 1, iy + 1, 1, nx, ny).astype(np.int32)
+    part = dict(x=ox.astype(R), y=oy.astype(R), z=np.zeros(n, R), ux=np.zeros(n, R),
+                uy=np.zeros(n, R), uz=np.zeros(n, R), w=np.full(n, p["we"], R), cell=cell)
+    order = np.argsort(cell, kind="stable")
+    part = {k: v[order] for k, v in part.items()}
+    F = np.zeros((nz + 2, ny + 2, nx + 2, 9))
+    jy = np.arange(ny + 2)
+    yc = ymin + (jy - 0.5) * float(p["dy"])
+    F[..., 1] = np.where(yc < -a, a, np.where(yc > a, -a, -yc))[None, :, None]
+    F[..., 5] = math.sqrt(20.0)
+    fields = F.reshape(-1, 9).astype(R)
+    if packed:
+        part = L.pack_particles(part, R, deck.vl)
+    return part, fields
+
+
 def initial_particles(deck: Deck) -> dict:
     if deck.name == "2stream-em":
         return default_particles(deck)
     if deck.name == "two-stream-1d":
         return two_stream_1d_particles(deck)
+    if deck.name == "diocotron":
+        return diocotron_state(deck)[0]
+    if deck.name == "diocotron-slab":
+        return diocotron_slab_state(deck)[0]
     return thermal_particles(deck)
+
+
+def initial_fields(deck: Deck, particles=None):
+    """Field members (num_cells, 9) at t = 0 for decks that start with fields,
+    else None (all zero, the reference's default Field_Initializer)."""
+    if deck.name == "diocotron":
+        return diocotron_state(deck)[1]
+    if deck.name == "diocotron-slab":
+        return diocotron_slab_state(deck)[1]
+    return None

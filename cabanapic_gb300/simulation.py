@@ -20,7 +20,7 @@ from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleLis
 class Simulation:
     def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
                  max_steps: int = None, time_push: bool = False, exact: bool = False,
-                 tiles: bool = True):
+                 tiles: bool = True, fields=None):
         self.deck = deck
         self.p = deck.derived()
         dev = torch.device(device if device is not None else "cuda")
@@ -36,6 +36,10 @@ class Simulation:
         if particles is None:
             particles = D.initial_particles(deck)
         self.particles.upload(particles)
+        if fields is None:
+            fields = D.initial_fields(deck)
+        if fields is not None:
+            self.fields.set_members(np.asarray(fields))
         self.sort_interval = int(sort_interval)
         self.sorter = pic.Sorter(self.particles, nc) if self.sort_interval > 0 else None
         cap = max_steps if max_steps is not None else max(deck.num_steps, 1)

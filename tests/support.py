@@ -74,16 +74,20 @@ def reorder_bound(acc_abs, count, eps):
     return 2.0 * k * eps * acc_abs.astype(np.float64) + 1e-30
 
 
-def oracle_run(orc, deck, packed, steps):
+def oracle_run(orc, deck, packed, steps, fields_init=None, out_state=None):
     """The reference's step sequence (example/example.cpp:221-266) in the
-    oracle from a given packed particle list; returns [steps, 2] energies
-    accumulated in double."""
+    oracle from a given packed particle list (and (num_cells, 9) initial field
+    members, default zero); returns [steps, 2] energies accumulated in double.
+    out_state, a dict, receives the final particle bytes and field members."""
     p = deck.derived()
     R = deck.R
     buf = packed.copy()
     nc = deck.num_cells
     g = orc.grid(deck.nx, deck.ny, deck.nz)
-    fields = np.zeros(L.cell_array_bytes(nc, 9, R) // np.dtype(R).itemsize, R)
+    if fields_init is None:
+        fields = np.zeros(L.cell_array_bytes(nc, 9, R) // np.dtype(R).itemsize, R)
+    else:
+        fields = L.pack_cells(np.asarray(fields_init, R), R)
     interp = np.zeros(L.cell_array_bytes(nc, 18, R) // np.dtype(R).itemsize, R)
     h = R(0.5)
     out = []
@@ -97,6 +101,9 @@ def oracle_run(orc, deck, packed, steps):
         orc.advance_e(fields, p["px"], p["py"], p["pz"], g, p["dt_eps0"])
         orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
         out.append(orc.energies(fields, g)[2:4])
+    if out_state is not None:
+        out_state["particles"] = buf
+        out_state["fields"] = L.unpack_cells(fields, nc, 9)
     return np.array(out)
 
 

@@ -99,3 +99,58 @@ def test_product_energy_rule_matches_the_oracle_restatement(orc):
         (pe, ee, le), (pb, eb, lb) = energies.two_stream_em_rule(gold, ours)
         (qe, fe, me, _), (qb, fb, mb, _) = energy_rule.two_stream_em_check(gold, ours)
         assert (pe, pb) == (qe, qb) and (ee, eb) == (fe, fb) and (le, lb) == (me, mb)
+
+
+def test_diocotron_initial_state():
+    """The column's t = 0 field solves the discrete Gauss law (backward-difference
+    div E at the nodes) for the particles' node charge plus the uniform
+    background; particles sit in the annulus, in cell order, drifting along
+    E x B."""
+    from oracle import diagnostics
+    nx, ny, nz = 32, 32, 8
+    d = decks.diocotron(n=(nx, ny, nz), ppc=16, dx=0.2, precision=8)
+    p, f = decks.diocotron_state(d)
+    par = d.derived()
+    dx, dy, dz = (float(par[k]) for k in ("dx", "dy", "dz"))
+    assert len(p["cell"]) == d.num_particles and d.num_particles % 32 == 0
+    assert np.all(np.diff(p["cell"]) >= 0)
+    rho = diagnostics.charge_density(p, nx, ny, nz, float(par["qsp"]), dx, dy, dz)[1:-1, 1:-1, 1:-1]
+    res = diagnostics.div_e(f, nx, ny, nz, dx, dy, dz) - (rho - rho.mean())
+    assert np.abs(res).max() < 1e-10 * np.abs(rho).max()
+    # the total charge is -n0 x annulus volume
+    rad = d.extra["radius"]
+    vol = np.pi * (0.35 ** 2 - 0.20 ** 2) * rad * rad * d.len_z_global
+    np.testing.assert_allclose(rho.sum() * dx * dy * dz, -vol, rtol=1e-3)
+    # u is perpendicular to E at the particle (cold E x B drift), z momentum zero
+    assert np.all(p["uz"] == 0)
+    X, Y, _ = (a * dx / 2 for a in _global(p, nx, ny, nz))
+    r = np.hypot(X - d.len_x_global / 2, Y - d.len_y_global / 2) / rad
+    assert r.min() > 0.2 - 1e-9 and r.max() < 0.35 + 1e-9
+    # the drift goes around the axis (the field of the periodic, discretised
+    # column is radial up to its images and the l = 3 ripple)
+    radial = (p["ux"] * (X - d.len_x_global / 2) + p["uy"] * (Y - d.len_y_global / 2)) / (r * rad)
+    speed = np.hypot(p["ux"], p["uy"])
+    assert np.abs(radial).mean() < 0.15 * speed.mean()
+
+
+def _global(p, nx, ny, nz):
+    ix, iy, iz = L.rank_to_index(p["cell"].astype(np.int64), nx, ny)
+    return (2.0 * (ix - 1) + (p["x"].astype(np.float64) + 1),
+            2.0 * (iy - 1) + (p["y"].astype(np.float64) + 1),
+            2.0 * (iz - 1) + (p["z"].astype(np.float64) + 1))
+
+
+def test_diocotron_slab_matches_reference_initializers():
+    """decks/dioctron_3d.cxx: 64 x 64 x 1, 5 per cell, strip |y| < a, first z
+    layer, at rest; E_y clamped shear and cB_z = sqrt(20)."""
+    d = decks.diocotron_slab(precision=8)
+    p, f = decks.diocotron_slab_state(d)
+    assert d.num_particles == 64 * 64 * 5
+    ix, iy, iz = L.rank_to_index(p["cell"].astype(np.int64), 64, 64)
+    assert np.all(iz == 1) and np.all(p["z"] == 0) and np.all(p["ux"] == 0)
+    ypos = -0.8 + (iy - 1 + (p["y"] + 1) / 2) * 0.025
+    assert np.abs(ypos).max() <= 0.1 + 1e-12
+    F = f.reshape(3, 66, 66, 9)
+    assert np.all(F[..., 5] == np.sqrt(20.0))
+    yc = -0.8 + (np.arange(66) - 0.5) * 0.025
+    np.testing.assert_array_equal(F[1, :, 7, 1], np.where(yc < -0.1, 0.1, np.where(yc > 0.1, -0.1, -yc)))
