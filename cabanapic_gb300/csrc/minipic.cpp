@@ -87,6 +87,9 @@ int main(int argc, char** argv) {
   Deck deck;
   const int num_steps = argc > 1 ? std::atoi(argv[1]) : deck.num_steps;
   const char* energies_path = argc > 2 ? argv[2] : "energies.txt";
+  // optional per-step particle and field dumps (example.cpp:131-132, 273-277)
+  FILE* fptr = argc > 3 ? std::fopen(argv[3], "w") : nullptr;
+  FILE* fpfd = argc > 4 ? std::fopen(argv[4], "w") : nullptr;
   try {
     const size_t nx = deck.nx, ny = deck.ny, nz = deck.nz, num_ghosts = deck.num_ghosts;
     const size_t num_cells = deck.num_cells;
@@ -115,6 +118,10 @@ int main(int argc, char** argv) {
     const real_t py = (ny > 1) ? frac * c * dt / dy : 0;
     const real_t pz = (nz > 1) ? frac * c * dt / dz : 0;
 
+    if (fptr) {
+      std::fprintf(fptr, "#step=0\n0 ");
+      dump_particles(fptr, particles, 0, 0, 0, dx, dy, dz, nx, ny, nz, num_ghosts);
+    }
     std::remove(energies_path);  // the reference only truncates at step 0
     for (int step = 1; step <= num_steps; step++) {
       load_interpolator_array(fields, interpolators, nx, ny, nz, num_ghosts);
@@ -127,7 +134,17 @@ int main(int argc, char** argv) {
       field_solver.advance_e(fields, px, py, pz, nx, ny, nz, num_ghosts, dt_eps0);
       field_solver.advance_b(fields, real_t(0.5) * px, real_t(0.5) * py, real_t(0.5) * pz, nx, ny, nz, num_ghosts);
       dump_energies(field_solver, fields, step, step * dt, px, py, pz, nx, ny, nz, num_ghosts, energies_path);
+      if (fpfd) {
+        std::fprintf(fpfd, "#step=%d\n", step);
+        field_solver.dump_fields(fpfd, fields, 0, 0, 0, dx, dy, dz, nx, ny, nz, num_ghosts);
+      }
+      if (fptr) {
+        std::fprintf(fptr, "#step=%d\n%e ", step, step * dt);
+        dump_particles(fptr, particles, 0, 0, 0, dx, dy, dz, nx, ny, nz, num_ghosts);
+      }
     }
+    if (fptr) std::fclose(fptr);
+    if (fpfd) std::fclose(fpfd);
     int32_t st = cpic::read_status();
     delete grid;
     if (st != 0) {

@@ -154,6 +154,12 @@ class EMFieldSolver:
         if fields is not None:
             self.init(fields)
 
+    def dump_fields(self, fp, fields: FieldArray, xmin, ymin, zmin, dx, dy, dz, nx, ny, nz, ng) -> None:
+        """Field_Solver::dump_fields (src/fields.h:318-350), synchronous."""
+        d = FieldDump(fields, nx)
+        d.enqueue(fields, xmin, dx, nx, ny, nz, ng, self.boundary)
+        d.write(fp)
+
     def init(self, fields: FieldArray) -> None:
         fields.buf.zero_()
 
@@ -244,6 +250,88 @@ def _g6(v: float) -> str:
 
 def _energy_line(step, time, e, b) -> str:
     return f"{step} {_g6(time)} {_g6(e)} {_g6(b)}"
+
+
+# ---------------------------------------------------------------- dumps
+def _fmt_pairs(vals: np.ndarray, sep: str, end: str) -> str:
+    """C printf "%e" of each value (Python's %e is the same format), pairs
+    joined as the reference's fprintf calls write them."""
+    v = vals.astype(np.float64).reshape(-1, 2)
+    return "".join(f"{a:e}{sep}{b:e}{end}" for a, b in v)
+
+
+class ParticleDump:
+    """Asynchronous dump_particles (src/helpers.h:31-61).  enqueue() computes
+    the printed values on the device and starts their copy into pinned host
+    memory on the stream; write() waits for that copy only and appends the
+    reference's line ("%e  %e " per particle, then a newline) to a file.  A
+    time loop enqueues at step k and writes before enqueueing at k + 1, so the
+    copy overlaps the next step's kernels."""
+
+    def __init__(self, particles: ParticleList):
+        R = torch.float32 if particles.precision == capi.CPIC_FLOAT else torch.float64
+        n = max(particles.n, 1)
+        self._dev = torch.empty(2 * n, dtype=R, device=particles.buf.device)
+        self._host = torch.empty(2 * n, dtype=R).pin_memory()
+        self._event = torch.cuda.Event()
+        self._pending = False
+        self._n = particles.n
+
+    def enqueue(self, particles: ParticleList, xmin, dx, nx, ny, nz, ng, boundary=Boundary.Periodic,
+                *, stream=None) -> None:
+        capi.load().call("cpic_particle_dump_values", particles.ptr, particles.n, particles.vl,
+                         C.byref(_grid(nx, ny, nz, ng, boundary)), particles.precision, float(xmin),
+                         float(dx), self._dev.data_ptr(), _stream(stream))
+        s = torch.cuda.current_stream() if stream is None else stream
+        with torch.cuda.stream(s):
+            self._host.copy_(self._dev, non_blocking=True)
+            self._event.record(s)
+        self._pending = True
+
+    def write(self, fp) -> None:
+        if not self._pending:
+            return
+        self._event.synchronize()
+        fp.write(_fmt_pairs(self._host[: 2 * self._n].numpy(), "  ", " ") + "\n")
+        self._pending = False
+
+
+def dump_particles(fp, particles: ParticleList, xmin, ymin, zmin, dx, dy, dz, nx, ny, nz, ng) -> None:
+    """dump_particles (src/helpers.h:31-61), synchronous: one line with the
+    x position and ux of every particle."""
+    d = ParticleDump(particles)
+    d.enqueue(particles, xmin, dx, nx, ny, nz, ng)
+    d.write(fp)
+
+
+class FieldDump:
+    """Asynchronous Field_Solver::dump_fields (src/fields.h:318-350): x and ex
+    along the first x row, "%e %e" lines then a blank line."""
+
+    def __init__(self, fields: FieldArray, nx: int):
+        R = torch.float32 if fields.precision == capi.CPIC_FLOAT else torch.float64
+        self._dev = torch.empty(2 * max(nx, 1), dtype=R, device=fields.buf.device)
+        self._host = torch.empty(2 * max(nx, 1), dtype=R).pin_memory()
+        self._event = torch.cuda.Event()
+        self._pending = False
+        self._nx = nx
+
+    def enqueue(self, fields: FieldArray, xmin, dx, nx, ny, nz, ng, boundary=Boundary.Periodic,
+                *, stream=None) -> None:
+        capi.load().call("cpic_field_dump_values", fields.ptr, C.byref(_grid(nx, ny, nz, ng, boundary)),
+                         fields.precision, float(xmin), float(dx), self._dev.data_ptr(), _stream(stream))
+        s = torch.cuda.current_stream() if stream is None else stream
+        with torch.cuda.stream(s):
+            self._host.copy_(self._dev, non_blocking=True)
+            self._event.record(s)
+        self._pending = True
+
+    def write(self, fp) -> None:
+        if not self._pending:
+            return
+        self._event.synchronize()
+        fp.write(_fmt_pairs(self._host[: 2 * self._nx].numpy(), " ", "\n") + "\n\n")
+        self._pending = False
 
 
 # ---------------------------------------------------------------- sort

@@ -11,6 +11,12 @@ step:
     step 0,
   * the charge-conservation residual max |(div E - rho/eps0)(t) - (...)(0)|
     relative to max |rho/eps0|,
+  * the field-energy error |W_a - W_b| / W_b of (a) against (b), W = 0.5 sum
+    (E^2 + cB^2) per step (the dump_energies quantity), its maximum over the
+    run, and the relative difference of the time averages over the second half
+    (a thermal plasma's field energy is a fluctuation level: once the two runs
+    decorrelate, the per-step values differ by the fluctuation itself while
+    the level agrees),
 and the pushes/s of (a) and (b).  The FP64 GPU build is the same arithmetic
 as the reference built with real_t = double; the tests check the two agree
 to round-off on short runs (tests/test_precision_gpu.py).
@@ -100,6 +106,12 @@ def run(cells=128, ppc=32, steps=1000, seed=2024, sample_every=1, sort_interval=
             rows.append(row)
     for s in sims.values():
         s.check_status()
+    w32 = sims["fp32"].energies().sum(axis=1)
+    w64 = sims["fp64"].energies().sum(axis=1)
+    werr = np.abs(w32 - w64) / np.where(w64 > 0, w64, 1.0)
+    half = slice(len(w64) // 2, None)
+    level = abs(float(w32[half].mean()) - float(w64[half].mean())) / float(w64[half].mean())
+    first_1e4 = next((i + 1 for i, e in enumerate(werr) if e > 1e-4), None)
     n = deck32.num_particles
     return {
         "config": f"thermal plasma {cells}^3 x {ppc} ppc = {n:,} particles, {steps} steps, seed {seed}",
@@ -107,6 +119,10 @@ def run(cells=128, ppc=32, steps=1000, seed=2024, sample_every=1, sort_interval=
         "pushes_per_s_fp64": n * steps / times["fp64"],
         "fp32_over_fp64": times["fp64"] / times["fp32"],
         "max_field_l2_rel": max(r["field_l2_rel"] for r in rows),
+        "field_energy_rel_err_max": float(werr.max()),
+        "field_energy_rel_err_final": float(werr[-1]),
+        "field_energy_first_step_above_1e-4": first_1e4,
+        "field_energy_level_rel_diff_second_half": level,
         "final": rows[-1],
         "rows": rows,
     }

@@ -4,8 +4,11 @@
 Each step: [cell sort every `sort_interval` steps] -> load_interpolator_array
 -> clear_accumulator_array -> push -> unload_accumulator_array -> advance_b(1/2)
 -> advance_e -> advance_b(1/2) -> field energies (double, kept on the device).
-The per-step particle and field text dumps of the reference are not part of
-the loop (example.cpp:274-277); energies are copied to the host on request.
+Energies are copied to the host on request.  With particle_dump / field_dump
+(open text files) the loop also writes the reference's per-step dumps
+(example.cpp:131-132, 273-277): each step's values are copied to pinned host
+memory asynchronously and written at the next step (or by flush_dumps()), so
+the copies overlap the following step's kernels.
 """
 from __future__ import annotations
 
@@ -20,7 +23,7 @@ from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleLis
 class Simulation:
     def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
                  max_steps: int = None, time_push: bool = False, exact: bool = False,
-                 tiles: bool = True, fields=None):
+                 tiles: bool = True, fields=None, particle_dump=None, field_dump=None):
         self.deck = deck
         self.p = deck.derived()
         dev = torch.device(device if device is not None else "cuda")
@@ -49,6 +52,17 @@ class Simulation:
         self.push_events = []
         self.exact = bool(exact)
         self.tiles = bool(tiles)
+        self.particle_dump = particle_dump
+        self.field_dump = field_dump
+        self._pdump = pic.ParticleDump(self.particles) if particle_dump is not None else None
+        self._fdump = pic.FieldDump(self.fields, deck.nx) if field_dump is not None else None
+        self._pending_step = None
+        if self._pdump is not None:
+            p = self.p
+            particle_dump.write("#step=0\n0 ")
+            self._pdump.enqueue(self.particles, 0, p["dx"], deck.nx, deck.ny, deck.nz, deck.num_ghosts,
+                                deck.boundary)
+            self._pdump.write(particle_dump)
 
     # ------------------------------------------------------------------
     def step(self) -> None:
@@ -77,7 +91,28 @@ class Simulation:
         self.solver.advance_b(self.fields, hpx, hpy, hpz, nx, ny, nz, ng)
         if self.step_no < self.energy.shape[0]:
             self.solver.energies_async(self.fields, nx, ny, nz, ng, out=self.energy[self.step_no])
+        if self._pdump is not None or self._fdump is not None:
+            self.flush_dumps()
+            if self._fdump is not None:
+                self._fdump.enqueue(self.fields, 0, p["dx"], nx, ny, nz, ng, d.boundary)
+            if self._pdump is not None:
+                self._pdump.enqueue(self.particles, 0, p["dx"], nx, ny, nz, ng, d.boundary)
+            self._pending_step = self.step_no + 1  # the reference's loop counts steps from 1
         self.step_no += 1
+
+    def flush_dumps(self) -> None:
+        """Writes the dumps enqueued at the last step (waits for their copies)."""
+        k = self._pending_step
+        if k is None:
+            return
+        if self._fdump is not None:
+            self.field_dump.write(f"#step={k}\n")
+            self._fdump.write(self.field_dump)
+        if self._pdump is not None:
+            t = float(self.deck.R(self.deck.R(k) * self.p["dt"]))
+            self.particle_dump.write(f"#step={k}\n{t:e} ")
+            self._pdump.write(self.particle_dump)
+        self._pending_step = None
 
     def run(self, steps: int) -> None:
         for _ in range(steps):

@@ -17,6 +17,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -273,6 +274,21 @@ class EM_Field_Solver {
   }
 };
 
+namespace cpic {
+// Device-computed dump values copied to the host (the reference deep-copies
+// the whole array first; only 2 reals per particle or x cell cross here).
+inline std::vector<real_t> dump_values(size_t n2, const char* what,
+                                       const std::function<int(void*)>& fill) {
+  DeviceBytes d(n2 * sizeof(real_t));
+  check(fill(d.get()), what);
+  std::vector<real_t> h(n2);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(current_stream());
+  check_cuda(cudaMemcpyAsync(h.data(), d.get(), n2 * sizeof(real_t), cudaMemcpyDeviceToHost, s), what);
+  check_cuda(cudaStreamSynchronize(s), what);
+  return h;
+}
+}  // namespace cpic
+
 // Field_Solver<Solver_Type>, src/fields.h:274-379: zeroes the fields on construction.
 template <class Solver_Type>
 class Field_Solver : public Solver_Type {
@@ -283,7 +299,31 @@ class Field_Solver : public Solver_Type {
                                      reinterpret_cast<cudaStream_t>(cpic::current_stream())),
                      "init_fields");
   }
+  // dump_fields, src/fields.h:318-350: x and ex along the first x row.
+  void dump_fields(FILE* fp, field_array_t& fields, real_t xmin, real_t, real_t, real_t dx, real_t,
+                   real_t, size_t nx, size_t ny, size_t nz, size_t ng) {
+    cpic_grid g = cpic::make_grid(nx, ny, nz, ng, cpic::field_boundary());
+    std::vector<real_t> v = cpic::dump_values(2 * nx, "dump_fields", [&](void* d) {
+      return cpic_field_dump_values(fields.data(), &g, cpic::kReal, xmin, dx, d, cpic::current_stream());
+    });
+    for (size_t i = 0; i < nx; ++i) fprintf(fp, "%e %e\n", v[2 * i], v[2 * i + 1]);
+    fprintf(fp, "\n\n");
+  }
 };
+
+// dump_particles, src/helpers.h:31-61: x position and ux of every particle.
+inline void dump_particles(FILE* fp, const particle_list_t& particles, const real_t xmin, const real_t,
+                           const real_t, const real_t dx, const real_t, const real_t, size_t nx,
+                           size_t ny, size_t nz, size_t ng) {
+  cpic_grid g = cpic::make_grid(nx, ny, nz, ng, Periodic);
+  const size_t n = particles.size();
+  std::vector<real_t> v = cpic::dump_values(2 * n, "dump_particles", [&](void* d) {
+    return cpic_particle_dump_values(particles.data(), (int64_t)n, particle_list_t::vector_length, &g,
+                                     cpic::kReal, xmin, dx, d, cpic::current_stream());
+  });
+  for (size_t i = 0; i < n; ++i) fprintf(fp, "%e  %e ", v[2 * i], v[2 * i + 1]);
+  fprintf(fp, "\n");
+}
 
 // dump_energies, src/fields.h:722-763: appends `step time E B` to energies.txt
 // (truncating at step 0), std::ostream default formatting.

@@ -192,6 +192,22 @@ int cpic_es_advance_e(void* fields, const cpic_grid* grid, double dt_eps0, int32
 int cpic_es_e_energy(const void* fields, const cpic_grid* grid, int32_t precision, double* d_out,
                      void* d_scratch, size_t scratch_bytes, cpic_stream_t stream);
 
+/* ---------------------------------------------------------------- dumps */
+/* Replaces the values printed by dump_particles (src/helpers.h:31-61):
+ * d_out[2p] = xmin + (ix - 1 + (x_p + 1) * 0.5) * dx (computed in double,
+ * stored as real_t), d_out[2p+1] = ux_p, for every particle p (2 * n real_t).
+ * The caller copies d_out to the host (asynchronously) and prints each pair
+ * as "%e  %e ", then one "\n". */
+int cpic_particle_dump_values(const void* particles, int64_t num_particles, int32_t particle_vl,
+                              const cpic_grid* grid, int32_t precision, double xmin, double dx,
+                              void* d_out, cpic_stream_t stream);
+
+/* Replaces the values printed by Field_Solver::dump_fields (src/fields.h:318-350):
+ * d_out[2(i-1)] = xmin + (i - 0.5) * dx, d_out[2(i-1)+1] = ex of voxel (i,1,1),
+ * i = 1..nx (2 * nx real_t); printed as "%e %e\n" per i, then "\n\n". */
+int cpic_field_dump_values(const void* fields, const cpic_grid* grid, int32_t precision, double xmin,
+                           double dx, void* d_out, cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- sort
  * Counting sort of the particle list by cell index, in place.  The reference
  * leaves this step commented out (example/example.cpp:226-228, Cabana::sortByKey);

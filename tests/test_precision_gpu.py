@@ -34,3 +34,5 @@ def test_small_precision_study_runs():
     assert abs(f["energy_drift_fp64"]) < 1e-2
     assert f["charge_err_fp64"] < 1e-11
     assert f["charge_err_fp32"] < 1e-4
+    assert 0 <= out["field_energy_rel_err_max"] < 1.0
+    assert out["field_energy_level_rel_diff_second_half"] < 0.2
