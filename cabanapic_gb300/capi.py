@@ -107,6 +107,8 @@ _SIGS = {
     "cpic_es_e_energy": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _vp, _vp, _sz, _vp]),
     "cpic_particle_dump_values": (_i32, [_vp, _i64, _i32, C.POINTER(CpicGrid), _i32, _f64, _f64, _vp, _vp]),
     "cpic_field_dump_values": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _f64, _f64, _vp, _vp]),
+    "cpic_sort_into_scratch_bytes": (_sz, [_i64, _i64, _i32, _i32]),
+    "cpic_sort_particles_into": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp, _sz, _vp]),
     "cpic_status_clear": (_i32, [_vp, _vp]),
     "cpic_status_read": (_i32, [_vp, _vp, C.POINTER(_i32)]),
 }

@@ -100,6 +100,49 @@ __device__ __forceinline__ bool warp_wait(unsigned long long* b, unsigned parity
   }
 }
 
+// Final step of a two-pass reduction, run by every thread of the last block:
+// partial b of value k is part[NV * b + k], b < nparts.  Thread t combines
+// partials t, t + THREADS, ... in that order, then a fixed shuffle tree and
+// thread 0 over the warps: the same order on every run (deterministic), and
+// the L2 loads of the partials are spread over the block instead of one
+// thread's dependent chain.  Bit k of max_mask selects max instead of sum.
+// res is valid in thread 0.
+template <int NV, int THREADS>
+__device__ __forceinline__ void reduce_partials(const double* __restrict__ part, unsigned nparts,
+                                                unsigned max_mask, double (&res)[NV]) {
+  __shared__ double sh[THREADS / 32][NV];
+  double v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = ((max_mask >> k) & 1u) ? -1.0e308 : 0.0;
+  for (unsigned b = threadIdx.x; b < nparts; b += THREADS) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double u = __ldcg(part + (size_t)NV * b + k);
+      v[k] = ((max_mask >> k) & 1u) ? fmax(v[k], u) : v[k] + u;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_xor_sync(kFull, v[k], o);
+      v[k] = ((max_mask >> k) & 1u) ? fmax(v[k], t) : v[k] + t;
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[threadIdx.x >> 5][k] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = sh[0][k];
+      for (int w = 1; w < THREADS / 32; ++w) t = ((max_mask >> k) & 1u) ? fmax(t, sh[w][k]) : t + sh[w][k];
+      res[k] = t;
+    }
+  }
+}
+
 inline int launch_status() {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CPIC_OK : CPIC_ECUDA;

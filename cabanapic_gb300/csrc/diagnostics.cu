@@ -139,17 +139,14 @@ __device__ void block_store_partials(double (&v)[NV], DiagScratch* sc, double* o
     last = (atomicAdd(&sc->done, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {  // block-uniform
     __threadfence();
-    for (int k = 0; k < NV; ++k) {
-      double t = __ldcg(&sc->part[k]);
-      for (unsigned b = 1; b < gridDim.x; ++b) {
-        const double u = __ldcg(&sc->part[NV * b + k]);
-        t = (want_max0 && k == 0) ? fmax(t, u) : t + u;
-      }
-      out[k] = (want_max0 && k == 0) ? t : t * scale;
+    double r[NV];
+    reduce_partials<NV, kDiagThreads>(sc->part, gridDim.x, want_max0 ? 1u : 0u, r);
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < NV; ++k) out[k] = (want_max0 && k == 0) ? r[k] : r[k] * scale;
+      sc->done = 0;
     }
-    sc->done = 0;
   }
 }
 

@@ -244,16 +244,15 @@ energy_kernel(const R* __restrict__ F, const GridDev g, double* __restrict__ out
     last = (prev == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {  // block-uniform
     __threadfence();
-    double te = 0.0, tb = 0.0;
-    for (unsigned k = 0; k < gridDim.x; ++k) {
-      te += __ldcg(&sc->part[2 * k]);
-      tb += __ldcg(&sc->part[2 * k + 1]);
+    double r[2];
+    reduce_partials<2, kThreads>(sc->part, gridDim.x, 0u, r);
+    if (threadIdx.x == 0) {
+      out[0] = r[0] * 0.5;
+      out[1] = r[1] * 0.5;
+      sc->done = 0;  // ready for the next call
     }
-    out[0] = te * 0.5;
-    out[1] = tb * 0.5;
-    sc->done = 0;  // ready for the next call
   }
 }
 
@@ -291,17 +290,20 @@ es_energy_kernel(const R* __restrict__ F, int num_cells, double* __restrict__ ou
     double t = 0.0;
     for (int k = 0; k < kThreads / 32; ++k) t += se[k];
     sc->part[2 * blockIdx.x] = t;
+    sc->part[2 * blockIdx.x + 1] = 0.0;
     __threadfence();
     last = (atomicAdd(&sc->done, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {  // block-uniform
     __threadfence();
-    double t = 0.0;
-    for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(&sc->part[2 * k]);
-    out[0] = t * 0.5;
-    out[1] = 0.0;
-    sc->done = 0;
+    double r[2];
+    reduce_partials<2, kThreads>(sc->part, gridDim.x, 0u, r);
+    if (threadIdx.x == 0) {
+      out[0] = r[0] * 0.5;
+      out[1] = 0.0;
+      sc->done = 0;
+    }
   }
 }
 

@@ -12,7 +12,10 @@
 //   2. scan:    exclusive prefix sum of the per-cell counts -> cell offsets
 //   3. scatter: perm[offset[cell] + rank] = particle index
 //   4. gather:  particles[d] = copy[perm[d]], member by member (coalesced writes)
-// The order within a cell depends on atomic arrival order.
+// The order within a cell depends on atomic arrival order.  The in-place
+// entry point gathers from a copy of the list in the scratch; the
+// out-of-place one (for callers with two lists) gathers straight into the
+// second list and skips that copy.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -169,9 +172,11 @@ gather_kernel(const unsigned char* __restrict__ src, unsigned char* __restrict__
   *reinterpret_cast<int*>(dst + L::cell_off(d)) = __ldg(reinterpret_cast<const int*>(src + L::cell_off(s)));
 }
 
+// dst == nullptr: in place, through the particle copy in the scratch;
+// otherwise src is gathered into dst (src unchanged, no copy).
 template <class R, int VL>
-static int sort_typed(void* particles, int n, int num_cells, const SortPlan& pl, unsigned char* sc,
-                      cudaStream_t s) {
+static int sort_typed(void* particles, void* dst, int n, int num_cells, const SortPlan& pl,
+                      unsigned char* sc, cudaStream_t s) {
   int* counts = reinterpret_cast<int*>(sc + pl.counts_off);
   int* sums = reinterpret_cast<int*>(sc + pl.sums_off);
   int* rank = reinterpret_cast<int*>(sc + pl.rank_off);
@@ -185,10 +190,27 @@ static int sort_typed(void* particles, int n, int num_cells, const SortPlan& pl,
   scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, pl.nscan_blocks);
   scan_add_kernel<<<(unsigned)pl.nscan_blocks, kScanThreads, 0, s>>>(counts, pl.nkeys, sums);
   scatter_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, n, num_cells, counts, rank, perm);
+  if (dst) {
+    gather_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, static_cast<unsigned char*>(dst), n, perm);
+    return launch_status();
+  }
   const size_t bytes = cpic_particle_list_bytes(n, sizeof(R), VL);
   if (cudaMemcpyAsync(copy, part, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return CPIC_ECUDA;
   gather_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(copy, part, n, perm);
   return launch_status();
+}
+
+static int sort_dispatch(void* particles, void* dst, int64_t num_particles, int64_t num_cells,
+                         int32_t precision, int32_t particle_vl, void* d_scratch, size_t need,
+                         size_t scratch_bytes, const SortPlan& pl, cudaStream_t s) {
+  if (scratch_bytes < need) return CPIC_ESCRATCH;
+  unsigned char* sc = static_cast<unsigned char*>(d_scratch);
+  const int n = (int)num_particles, nc = (int)num_cells;
+  if (precision == CPIC_FLOAT)
+    return particle_vl == 32 ? sort_typed<float, 32>(particles, dst, n, nc, pl, sc, s)
+                             : sort_typed<float, 16>(particles, dst, n, nc, pl, sc, s);
+  return particle_vl == 32 ? sort_typed<double, 32>(particles, dst, n, nc, pl, sc, s)
+                           : sort_typed<double, 16>(particles, dst, n, nc, pl, sc, s);
 }
 
 }  // namespace cpic
@@ -214,13 +236,31 @@ extern "C" int cpic_sort_particles(void* particles, int64_t num_particles, int64
   if (!particles || !d_scratch) return CPIC_EINVAL;
   if (((uintptr_t)particles & 15) || ((uintptr_t)d_scratch & 255)) return CPIC_EINVAL;
   const SortPlan pl = plan_sort(num_particles, num_cells, precision, particle_vl);
-  if (scratch_bytes < pl.total) return CPIC_ESCRATCH;
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  unsigned char* sc = static_cast<unsigned char*>(d_scratch);
-  const int n = (int)num_particles, nc = (int)num_cells;
-  if (precision == CPIC_FLOAT)
-    return particle_vl == 32 ? sort_typed<float, 32>(particles, n, nc, pl, sc, s)
-                             : sort_typed<float, 16>(particles, n, nc, pl, sc, s);
-  return particle_vl == 32 ? sort_typed<double, 32>(particles, n, nc, pl, sc, s)
-                           : sort_typed<double, 16>(particles, n, nc, pl, sc, s);
+  return sort_dispatch(particles, nullptr, num_particles, num_cells, precision, particle_vl, d_scratch,
+                       pl.total, scratch_bytes, pl, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" size_t cpic_sort_into_scratch_bytes(int64_t num_particles, int64_t num_cells, int32_t precision,
+                                               int32_t particle_vl) {
+  if (num_particles < 0 || num_cells < 1) return 0;
+  if (precision != CPIC_FLOAT && precision != CPIC_DOUBLE) return 0;
+  if (particle_vl != 16 && particle_vl != 32) return 0;
+  return plan_sort(num_particles, num_cells, precision, particle_vl).copy_off;
+}
+
+extern "C" int cpic_sort_particles_into(const void* particles, void* sorted, int64_t num_particles,
+                                        int64_t num_cells, int32_t precision, int32_t particle_vl,
+                                        void* d_scratch, size_t scratch_bytes, cpic_stream_t stream) {
+  if (precision != CPIC_FLOAT && precision != CPIC_DOUBLE) return CPIC_EINVAL;
+  if (particle_vl != 16 && particle_vl != 32) return CPIC_EINVAL;
+  if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
+  if (num_cells < 1 || num_cells > 0x7fffffffLL - 64) return CPIC_EINVAL;
+  if (num_particles == 0) return CPIC_OK;
+  if (!particles || !sorted || !d_scratch || particles == sorted) return CPIC_EINVAL;
+  if (((uintptr_t)particles & 15) || ((uintptr_t)sorted & 15) || ((uintptr_t)d_scratch & 255))
+    return CPIC_EINVAL;
+  const SortPlan pl = plan_sort(num_particles, num_cells, precision, particle_vl);
+  return sort_dispatch(const_cast<void*>(particles), sorted, num_particles, num_cells, precision,
+                       particle_vl, d_scratch, pl.copy_off, scratch_bytes, pl,
+                       reinterpret_cast<cudaStream_t>(stream));
 }

@@ -336,21 +336,35 @@ class FieldDump:
 
 # ---------------------------------------------------------------- sort
 class Sorter:
-    """Counting sort of a particle list by cell (scratch owned by this object)."""
+    """Counting sort of a particle list by cell (scratch owned by this object).
 
-    def __init__(self, particles: ParticleList, num_cells: int):
+    double_buffer=True keeps a second particle buffer instead of the in-place
+    sort's copy: each sort gathers into it and the list swaps buffers (same
+    memory, one 2 x list-size copy less per sort).  The list's buffer object
+    changes; hold the ParticleList, not its buffer."""
+
+    def __init__(self, particles: ParticleList, num_cells: int, double_buffer: bool = False):
         lib = capi.load()
         self.num_cells = int(num_cells)
-        nbytes = lib.raw("cpic_sort_scratch_bytes")(particles.n, self.num_cells, particles.precision,
-                                                   particles.vl)
+        self.double_buffer = bool(double_buffer)
+        fn = "cpic_sort_into_scratch_bytes" if self.double_buffer else "cpic_sort_scratch_bytes"
+        nbytes = lib.raw(fn)(particles.n, self.num_cells, particles.precision, particles.vl)
         if nbytes == 0:
-            raise capi.CpicError("cpic_sort_scratch_bytes", capi.CPIC_EINVAL, "bad arguments")
+            raise capi.CpicError(fn, capi.CPIC_EINVAL, "bad arguments")
         self.scratch = torch.empty(nbytes, dtype=torch.uint8, device=particles.buf.device)
+        self.spare = torch.empty_like(particles.buf) if self.double_buffer else None
 
     def __call__(self, particles: ParticleList, *, stream=None) -> None:
-        capi.load().call("cpic_sort_particles", particles.ptr, particles.n, self.num_cells,
-                         particles.precision, particles.vl, self.scratch.data_ptr(),
-                         self.scratch.numel(), _stream(stream))
+        lib = capi.load()
+        if self.double_buffer:
+            lib.call("cpic_sort_particles_into", particles.ptr, self.spare.data_ptr(), particles.n,
+                     self.num_cells, particles.precision, particles.vl, self.scratch.data_ptr(),
+                     self.scratch.numel(), _stream(stream))
+            particles.buf, self.spare = self.spare, particles.buf
+            return
+        lib.call("cpic_sort_particles", particles.ptr, particles.n, self.num_cells,
+                 particles.precision, particles.vl, self.scratch.data_ptr(), self.scratch.numel(),
+                 _stream(stream))
 
 
 def sort_particles(particles: ParticleList, num_cells: int, *, stream=None) -> None:

@@ -44,7 +44,8 @@ class Simulation:
         if fields is not None:
             self.fields.set_members(np.asarray(fields))
         self.sort_interval = int(sort_interval)
-        self.sorter = pic.Sorter(self.particles, nc) if self.sort_interval > 0 else None
+        self.sorter = (pic.Sorter(self.particles, nc, double_buffer=True) if self.sort_interval > 0
+                       else None)
         cap = max_steps if max_steps is not None else max(deck.num_steps, 1)
         self.energy = torch.zeros((cap, 2), dtype=torch.float64, device=dev)
         self.step_no = 0
