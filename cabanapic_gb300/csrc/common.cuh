@@ -12,11 +12,34 @@ namespace cpic {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kCellBlock = CPIC_CELL_BLOCK;
 
+// Division by a fixed d >= 1 for 0 <= n < 2^31: q = (n * m) >> (31 + l) with
+// l = ceil(log2 d) and m = ceil(2^(31 + l) / d) < 2^32.  Exact: the product is
+// n / d plus less than n / 2^(31 + l) < 1 / d, which never reaches the next
+// integer.
+struct DivMagic {
+  unsigned m;
+  int shift;  // 31 + l
+};
+
+inline DivMagic make_div_magic(unsigned d) {
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  DivMagic r;
+  r.m = (unsigned)(((1ull << (31 + l)) + d - 1) / d);
+  r.shift = 31 + l;
+  return r;
+}
+
+__device__ __forceinline__ int div_magic(int n, DivMagic q) {
+  return (int)(((unsigned long long)(unsigned)n * q.m) >> q.shift);
+}
+
 // Ghosted grid extents and VOXEL (src/types.h:195).
 struct GridDev {
   int nx, ny, nz;   // interior cells
   int sx, sy, sz;   // ghosted extents (n + 2)
   int num_cells;    // sx * sy * sz
+  DivMagic dsx, dsy;  // division by sx and sy (RANK_TO_INDEX)
   __host__ __device__ int vox(int x, int y, int z) const { return x + sx * (y + sy * z); }
 };
 
@@ -25,6 +48,8 @@ inline GridDev make_grid(const cpic_grid* g) {
   d.nx = (int)g->nx; d.ny = (int)g->ny; d.nz = (int)g->nz;
   d.sx = d.nx + 2; d.sy = d.ny + 2; d.sz = d.nz + 2;
   d.num_cells = d.sx * d.sy * d.sz;
+  d.dsx = make_div_magic((unsigned)d.sx);
+  d.dsy = make_div_magic((unsigned)d.sy);
   return d;
 }
 

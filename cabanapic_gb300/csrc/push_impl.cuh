@@ -257,10 +257,10 @@ __device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R 
     if (axis == 3) { done = true; break; }
 
     const R fs = (axis == 0) ? dirx : (axis == 1) ? diry : dirz;
-    // RANK_TO_INDEX (src/types.h:184-193)
+    // RANK_TO_INDEX (src/types.h:184-193); cell is in [0, num_cells) here
     int ix = cell, iy, iz;
-    iy = ix / g.sx; ix -= iy * g.sx;
-    iz = iy / g.sy; iy -= iz * g.sy;
+    iy = div_magic(ix, g.dsx); ix -= iy * g.sx;
+    iz = div_magic(iy, g.dsy); iy -= iz * g.sy;
     const int step = fs > 0 ? 1 : -1;
     if (axis == 0) ix += step; else if (axis == 1) iy += step; else iz += step;
     // detect_leaving_domain (move_p.h:9-54): the last matching test wins
@@ -634,7 +634,8 @@ __device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __res
   }
 }
 
-constexpr int kConsumers = kWarps - 1;  // warps 1..7 push; warp 0 stages windows
+constexpr int kTiledThreads = 512;                // tiled kernel: 16 warps per CTA
+constexpr int kConsumers = kTiledThreads / 32 - 1;  // warps 1..15 push; warp 0 stages windows
 
 template <class R>
 constexpr size_t tiled_dyn_smem(int wxmax) {
@@ -660,7 +661,7 @@ __device__ __forceinline__ int tile_sample(const unsigned char* __restrict__ par
 // empty[j % 2].  No CTA-wide barrier: a warp delayed by a queue drain holds up
 // nobody until the producer needs its buffer again.
 template <class R, int VL, bool LITERAL, bool FAST>
-__global__ void __launch_bounds__(kPushThreads, sizeof(R) == 4 ? 4 : 2)  // FP32: 64 registers
+__global__ void __launch_bounds__(kTiledThreads, sizeof(R) == 4 ? 2 : 1)  // FP32: 64 registers
 push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
                   R* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status,
                   int chunks_per_warp, int wxmax) {
@@ -774,22 +775,22 @@ int launch_push(void* particles, int n, const void* interp, void* acc, const Pus
   return launch_status();
 }
 
-// Tile shape: 4 chunks per consumer warp (896 particles).  Each tile sizes its
-// own window from its sampled cells (a run of 896 / ppc voxels plus margins),
-// so the shape does not depend on the mean particle density, which says little
-// when particles fill part of the box; wxmax only bounds the shared memory.
-// Two windows of 9 x 21 rows take 30.2 KB in FP32, 46.4 KB per CTA with the
-// mover queues: four CTAs fit the 196 KB shared-memory carveout and leave
-// 60 KB of L1 (24 rows tip them into the 228 KB carveout, 28 KB of L1, and
-// the push was measured 9% slower).  Runs longer than wxmax - 2 voxels (under
-// ~47 particles per cell) get a window centred on the median sample and the
-// rest of the tile gathers from global memory.
+// Tile shape: 4 chunks per consumer warp (1920 particles).  Each tile sizes
+// its own window from its sampled cells (a run of 1920 / ppc voxels plus
+// margins), so the shape does not depend on the mean particle density, which
+// says little when particles fill part of the box; wxmax only bounds the
+// shared memory.  Two windows of 9 x 36 rows take 51.8 KB in FP32, 86.4 KB
+// per CTA with the 15 mover queues: two CTAs fit the 196 KB shared-memory
+// carveout and leave 60 KB of L1 (crossing into the 228 KB carveout, 28 KB of
+// L1, was measured 9% slower).  Runs longer than wxmax - 2 voxels (under ~57
+// particles per cell) get a window centred on the median sample and the rest
+// of the tile gathers from global memory.
 struct TileShape {
   int chunks_per_warp, wxmax;
 };
 
 inline TileShape tile_shape(const GridDev& g) {
-  TileShape ts{4, 21};
+  TileShape ts{4, 36};
   if (ts.wxmax > g.sx) ts.wxmax = g.sx;  // segments of one window must not overlap
   if (ts.wxmax < 3) ts.wxmax = 3;
   return ts;
@@ -814,7 +815,7 @@ int launch_push_tiled(void* particles, int n, const void* interp, void* acc, con
   }
   if (occ_dyn[dev] != dyn) {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kPushThreads, dyn) != cudaSuccess || b < 1) b = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kTiledThreads, dyn) != cudaSuccess || b < 1) b = 1;
     occ_blocks[dev] = b;
     occ_dyn[dev] = dyn;
   }
@@ -823,7 +824,7 @@ int launch_push_tiled(void* particles, int n, const void* interp, void* acc, con
   int64_t blocks = (int64_t)sm_count() * occ_blocks[dev];
   if (blocks > ntiles) blocks = ntiles;
   if (blocks < 1) blocks = 1;
-  kern<<<(unsigned)blocks, kPushThreads, dyn, s>>>(static_cast<unsigned char*>(particles), n,
+  kern<<<(unsigned)blocks, kTiledThreads, dyn, s>>>(static_cast<unsigned char*>(particles), n,
                                                   static_cast<const R*>(interp), static_cast<R*>(acc), a,
                                                   status, ts.chunks_per_warp, ts.wxmax);
   return launch_status();
