@@ -213,9 +213,22 @@ __device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool
   }
 }
 
+// Twice the fractional distance to a face, (dir - p) / s (move_p.h:115-117).
+// FAST (FP32): the hardware division, within 2 ulp; two faces closer than
+// that may then be crossed in the other order, with a streak of ~1e-7 of the
+// displacement between them.  Displacements below 1e-30 count as none.
+template <class R, bool FAST>
+__device__ __forceinline__ R face_fraction(R dir, R p, R s) {
+  if constexpr (sizeof(R) == 4 && FAST) {
+    return (fabsf(s) < 1e-30f) ? R(3.4e38) : __fdividef(dir - p, s);
+  } else {
+    return (s == 0) ? R(3.4e38) : (dir - p) / s;
+  }
+}
+
 // move_p for one particle (src/move_p.h:93-371), positions and displacement in
 // registers; writes the final offsets and cell of particle `pidx`.
-template <class R, int VL>
+template <class R, int VL, bool FAST>
 __device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R py, R pz, R dx,
                                       R dy, R dz, R q, int cell, int pidx, R* __restrict__ acc,
                                       const GridDev g, int* __restrict__ status) {
@@ -233,9 +246,9 @@ __device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R 
     const R diry = (sy > 0) ? R(1) : R(-1);
     const R dirz = (sz > 0) ? R(1) : R(-1);
     // twice the fractional distance to each face (move_p.h:115-117)
-    const R fx = (sx == 0) ? R(3.4e38) : (dirx - px) / sx;
-    const R fy = (sy == 0) ? R(3.4e38) : (diry - py) / sy;
-    const R fz = (sz == 0) ? R(3.4e38) : (dirz - pz) / sz;
+    const R fx = face_fraction<R, FAST>(dirx, px, sx);
+    const R fy = face_fraction<R, FAST>(diry, py, sy);
+    const R fz = face_fraction<R, FAST>(dirz, pz, sz);
     R len = 2;
     int axis = 3;
     if (fx < len) { len = fx; axis = 0; }
@@ -482,7 +495,7 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
       const int cc = Q.cell[s], ii = Q.idx[s];
       __syncwarp();
       qn -= 32;
-      move_one<R, VL>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, status);
+      move_one<R, VL, FAST>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, status);
     }
   }
 }
@@ -500,19 +513,19 @@ __device__ __forceinline__ LaneCtx make_lane_ctx() {
   return lc;
 }
 
-template <class R, int VL>
+template <class R, int VL, bool FAST>
 __device__ __forceinline__ void drain_queue(unsigned char* __restrict__ part, MoverQueue<R>& Q, int qn,
                                             int lane, const PushArgs<R>& a, R* __restrict__ acc,
                                             int* __restrict__ status) {
   __syncwarp();
   if (lane < qn)
-    move_one<R, VL>(part, Q.px[lane], Q.py[lane], Q.pz[lane], Q.dx[lane], Q.dy[lane], Q.dz[lane],
+    move_one<R, VL, FAST>(part, Q.px[lane], Q.py[lane], Q.pz[lane], Q.dx[lane], Q.dy[lane], Q.dz[lane],
                     Q.q[lane], Q.cell[lane], Q.idx[lane], acc, a.g, status);
 }
 
 // ------------------------------------------------------------ streaming kernel
 template <class R, int VL, bool LITERAL, bool FAST>
-__global__ void __launch_bounds__(kPushThreads)
+__global__ void __launch_bounds__(kPushThreads, sizeof(R) == 4 ? 4 : 2)  // FP32: 64 registers
 push_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
             R* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status) {
   constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
@@ -537,7 +550,7 @@ push_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ inter
                                             nullptr, nowin, 0, 0);
     cur = nxt;
   }
-  drain_queue<R, VL>(part, Q, qn, lc.lane, a, acc, status);
+  drain_queue<R, VL, FAST>(part, Q, qn, lc.lane, a, acc, status);
 }
 
 // ------------------------------------------------------------ tiled kernel
@@ -748,7 +761,7 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
     if (lc.lane == 0) mbar_arrive(&empty[b]);
   }
   if (!ok && lc.lane == 0) atomicOr(status, CPIC_STATUS_PIPELINE);
-  drain_queue<R, VL>(part, Q, qn, lc.lane, a, acc, status);
+  drain_queue<R, VL, FAST>(part, Q, qn, lc.lane, a, acc, status);
 }
 
 // ------------------------------------------------------------ host side
