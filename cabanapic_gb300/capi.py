@@ -29,6 +29,7 @@ CPIC_DOUBLE = 8
 CPIC_PUSH_TRUE_SQRT = 1
 CPIC_PUSH_EXACT = 2
 CPIC_PUSH_STREAMING = 4
+CPIC_PUSH_ACC_F64 = 8
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -109,6 +110,7 @@ _SIGS = {
     "cpic_field_dump_values": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _f64, _f64, _vp, _vp]),
     "cpic_sort_into_scratch_bytes": (_sz, [_i64, _i64, _i32, _i32]),
     "cpic_sort_particles_into": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp, _sz, _vp]),
+    "cpic_unload_accumulator_f64": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64, _i32, _vp]),
     "cpic_status_clear": (_i32, [_vp, _vp]),
     "cpic_status_read": (_i32, [_vp, _vp, C.POINTER(_i32)]),
 }

@@ -75,18 +75,18 @@ load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridD
 
 // ------------------------------------------------------------ accumulator
 // unload_accumulator_array (accumulator.cpp:71-110): cells [1, n+1] per axis.
-template <class R>
+template <class R, class Acc = R>
 __global__ void __launch_bounds__(kThreads)
-unload_kernel(R* __restrict__ F, const R* __restrict__ A, const GridDev g, R cx, R cy, R cz) {
+unload_kernel(R* __restrict__ F, const Acc* __restrict__ A, const GridDev g, Acc cx, Acc cy, Acc cz) {
   int x, y, z;
   if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx + 1, g.ny + 1, g.nz + 1, x, y, z)) return;
   const int i = g.vox(x, y, z);
   const int xd = g.vox(x - 1, y, z), yd = g.vox(x, y - 1, z), zd = g.vox(x, y, z - 1);
   const int xzd = g.vox(x - 1, y, z - 1), xyd = g.vox(x - 1, y - 1, z), yzd = g.vox(x, y - 1, z - 1);
   auto a = [&](int c, int k) { return __ldg(A + (size_t)c * 12 + k); };
-  F[cell_at<9>(i, CPIC_F_JFX)] = cx * (a(i, 0) + a(yd, 1) + a(zd, 2) + a(yzd, 3));
-  F[cell_at<9>(i, CPIC_F_JFY)] = cy * (a(i, 4) + a(zd, 5) + a(xd, 6) + a(xzd, 7));
-  F[cell_at<9>(i, CPIC_F_JFZ)] = cz * (a(i, 8) + a(xd, 9) + a(yd, 10) + a(xyd, 11));
+  F[cell_at<9>(i, CPIC_F_JFX)] = (R)(cx * (a(i, 0) + a(yd, 1) + a(zd, 2) + a(yzd, 3)));
+  F[cell_at<9>(i, CPIC_F_JFY)] = (R)(cy * (a(i, 4) + a(zd, 5) + a(xd, 6) + a(xzd, 7)));
+  F[cell_at<9>(i, CPIC_F_JFZ)] = (R)(cz * (a(i, 8) + a(xd, 9) + a(yd, 10) + a(xyd, 11)));
 }
 
 // ------------------------------------------------------------ ghosts
@@ -315,7 +315,7 @@ static int typed_load_interp(const void* f, void* i, const GridDev& g, cudaStrea
   return launch_status();
 }
 
-template <class R>
+template <class R, class Acc = R>
 static int typed_unload(void* f, const void* a, const GridDev& g, double dx, double dy, double dz,
                         double dt, cudaStream_t s) {
   const R rdx = (R)dx, rdy = (R)dy, rdz = (R)dz, rdt = (R)dt;
@@ -324,8 +324,8 @@ static int typed_unload(void* f, const void* a, const GridDev& g, double dx, dou
   const R cy = (R)(0.25 / (double)(R)(rdz * rdx * rdt));
   const R cz = (R)(0.25 / (double)(R)(rdx * rdy * rdt));
   const int64_t n = (int64_t)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
-  unload_kernel<R><<<blocks_for(n), kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const R*>(a), g,
-                                                      cx, cy, cz);
+  unload_kernel<R, Acc><<<blocks_for(n), kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const Acc*>(a),
+                                                           g, (Acc)cx, (Acc)cy, (Acc)cz);
   return launch_status();
 }
 
@@ -432,6 +432,19 @@ extern "C" int cpic_unload_accumulator(void* fields, const void* accumulators, c
   const GridDev g = make_grid(grid);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   return precision == CPIC_FLOAT ? typed_unload<float>(fields, accumulators, g, dx, dy, dz, dt, s)
+                                 : typed_unload<double>(fields, accumulators, g, dx, dy, dz, dt, s);
+}
+
+extern "C" int cpic_unload_accumulator_f64(void* fields, const double* accumulators, const cpic_grid* grid,
+                                           double dx, double dy, double dz, double dt, int32_t precision,
+                                           cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields || !accumulators) return CPIC_EINVAL;
+  const GridDev g = make_grid(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return precision == CPIC_FLOAT ? typed_unload<float, double>(fields, accumulators, g, dx, dy, dz, dt, s)
                                  : typed_unload<double>(fields, accumulators, g, dx, dy, dz, dt, s);
 }
 

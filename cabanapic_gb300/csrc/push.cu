@@ -23,7 +23,8 @@ extern "C" int cpic_push(void* particles, int64_t num_particles, const void* int
   if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
   if (prm->precision != CPIC_FLOAT && prm->precision != CPIC_DOUBLE) return CPIC_EINVAL;
   if (prm->particle_vl != 16 && prm->particle_vl != 32) return CPIC_EINVAL;
-  if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT | CPIC_PUSH_STREAMING)) return CPIC_EINVAL;
+  if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT | CPIC_PUSH_STREAMING | CPIC_PUSH_ACC_F64))
+    return CPIC_EINVAL;
   if (num_particles == 0) return CPIC_OK;
   if (!particles || !interpolators || !accumulators) return CPIC_EINVAL;
   if (((uintptr_t)accumulators & 15) || ((uintptr_t)particles & 15) ||

@@ -173,10 +173,19 @@ __device__ __forceinline__ int value_of_lane(int lane) {
   return ((lane & 16) ? 6 : 0) + ((lane & 8) ? 3 : 0) + j;
 }
 
+// Adds 12 deposits to one accumulator row (16-byte vector reductions for
+// FP32 rows; FP64 rows, the compensated accumulation, take scalar atomics).
+template <class R, class Acc>
+__device__ __forceinline__ void red_add12(Acc* __restrict__ a, const R v[12]) {
+  red_add4(a + 0, (Acc)v[0], (Acc)v[1], (Acc)v[2], (Acc)v[3]);
+  red_add4(a + 4, (Acc)v[4], (Acc)v[5], (Acc)v[6], (Acc)v[7]);
+  red_add4(a + 8, (Acc)v[8], (Acc)v[9], (Acc)v[10], (Acc)v[11]);
+}
+
 // Deposit of the in-cell particles of one warp into accumulator_array.  `dep`
 // lanes add v[0..11] to accumulator row `cell`; `vi` is value_of_lane(lane).
-template <class R>
-__device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool dep,
+template <class R, class Acc>
+__device__ __forceinline__ void warp_deposit(Acc* __restrict__ acc, int cell, bool dep,
                                              const R v[12], int lane, int vi) {
   const unsigned dm = __ballot_sync(kFull, dep);
   if (dm == 0u) return;
@@ -186,7 +195,7 @@ __device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool
 #pragma unroll
     for (int k = 0; k < 12; ++k) w[k] = dep ? v[k] : R(0);
     const R tot = reduce_scatter12<R>(w, lane);
-    if (vi >= 0) red_add(acc + (size_t)cell0 * 12 + vi, tot);
+    if (vi >= 0) red_add(acc + (size_t)cell0 * 12 + vi, (Acc)tot);
     return;
   }
   const int key = dep ? cell : -1 - lane;
@@ -203,14 +212,9 @@ __device__ __forceinline__ void warp_deposit(R* __restrict__ acc, int cell, bool
     for (int k = 0; k < 12; ++k) w[k] = in_major ? v[k] : R(0);
     const R tot = reduce_scatter12<R>(w, lane);
     const int major_cell = __shfl_sync(kFull, cell, leader);
-    if (vi >= 0) red_add(acc + (size_t)major_cell * 12 + vi, tot);
+    if (vi >= 0) red_add(acc + (size_t)major_cell * 12 + vi, (Acc)tot);
   }
-  if (dep && !in_major) {
-    R* a = acc + (size_t)cell * 12;
-    red_add4(a + 0, v[0], v[1], v[2], v[3]);
-    red_add4(a + 4, v[4], v[5], v[6], v[7]);
-    red_add4(a + 8, v[8], v[9], v[10], v[11]);
-  }
+  if (dep && !in_major) red_add12(acc + (size_t)cell * 12, v);
 }
 
 // Twice the fractional distance to a face, (dir - p) / s (move_p.h:115-117).
@@ -228,9 +232,9 @@ __device__ __forceinline__ R face_fraction(R dir, R p, R s) {
 
 // move_p for one particle (src/move_p.h:93-371), positions and displacement in
 // registers; writes the final offsets and cell of particle `pidx`.
-template <class R, int VL, bool FAST>
+template <class R, int VL, bool FAST, class Acc>
 __device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R py, R pz, R dx,
-                                      R dy, R dz, R q, int cell, int pidx, R* __restrict__ acc,
+                                      R dy, R dz, R q, int cell, int pidx, Acc* __restrict__ acc,
                                       const GridDev g, int* __restrict__ status) {
   using L = PLayout<R, VL>;
   if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) atomicOr(status, CPIC_STATUS_NONFINITE);
@@ -261,10 +265,7 @@ __device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R 
     const R corr = (R)((double)(q * sx * sy * sz) * (1. / 3.));
     R v[12];
     currents12<R>(q, sx, sy, sz, mx, my, mz, corr, v);
-    R* a = acc + (size_t)cell * 12;
-    red_add4(a + 0, v[0], v[1], v[2], v[3]);
-    red_add4(a + 4, v[4], v[5], v[6], v[7]);
-    red_add4(a + 8, v[8], v[9], v[10], v[11]);
+    red_add12(acc + (size_t)cell * 12, v);
     dx -= sx; dy -= sy; dz -= sz;
     px += sx + sx; py += sy + sy; pz += sz + sz;
     if (axis == 3) { done = true; break; }
@@ -420,10 +421,10 @@ __device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, i
 // One 32-particle chunk: gather, Boris, in-cell move and deposit, queueing of
 // the crossers.  TILED gathers from the shared-memory window `wbuf` when the
 // particle's cell has a slot in window `w`.
-template <class R, int VL, bool LITERAL, bool FAST, bool TILED>
+template <class R, int VL, bool LITERAL, bool FAST, bool TILED, class Acc>
 __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int n, int chunk,
                                            const PState<R>& cur, const R* __restrict__ interp,
-                                           R* __restrict__ acc, const PushArgs<R>& a,
+                                           Acc* __restrict__ acc, const PushArgs<R>& a,
                                            int* __restrict__ status, MoverQueue<R>& Q, int& qn,
                                            const LaneCtx& lc, const R* __restrict__ wbuf,
                                            const TileWin& w, int ys, int zs) {
@@ -474,7 +475,7 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
   R v[12];
   const R corr = q * ux * uy * uz * one_third;
   currents12<R>(q, ux, uy, uz, mx, my, mz, corr, v);
-  warp_deposit<R>(acc, cell, inb, v, lc.lane, lc.vi);
+  warp_deposit<R, Acc>(acc, cell, inb, v, lc.lane, lc.vi);
 
   // compact the cell-crossing particles into the warp queue
   const bool cross = valid && !inb;
@@ -495,7 +496,7 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
       const int cc = Q.cell[s], ii = Q.idx[s];
       __syncwarp();
       qn -= 32;
-      move_one<R, VL, FAST>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, status);
+      move_one<R, VL, FAST, Acc>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, status);
     }
   }
 }
@@ -513,21 +514,21 @@ __device__ __forceinline__ LaneCtx make_lane_ctx() {
   return lc;
 }
 
-template <class R, int VL, bool FAST>
+template <class R, int VL, bool FAST, class Acc>
 __device__ __forceinline__ void drain_queue(unsigned char* __restrict__ part, MoverQueue<R>& Q, int qn,
-                                            int lane, const PushArgs<R>& a, R* __restrict__ acc,
+                                            int lane, const PushArgs<R>& a, Acc* __restrict__ acc,
                                             int* __restrict__ status) {
   __syncwarp();
   if (lane < qn)
-    move_one<R, VL, FAST>(part, Q.px[lane], Q.py[lane], Q.pz[lane], Q.dx[lane], Q.dy[lane], Q.dz[lane],
+    move_one<R, VL, FAST, Acc>(part, Q.px[lane], Q.py[lane], Q.pz[lane], Q.dx[lane], Q.dy[lane], Q.dz[lane],
                     Q.q[lane], Q.cell[lane], Q.idx[lane], acc, a.g, status);
 }
 
 // ------------------------------------------------------------ streaming kernel
-template <class R, int VL, bool LITERAL, bool FAST>
+template <class R, int VL, bool LITERAL, bool FAST, class Acc>
 __global__ void __launch_bounds__(kPushThreads, sizeof(R) == 4 ? 4 : 2)  // FP32: 64 registers
 push_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
-            R* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status) {
+            Acc* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status) {
   constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
   __shared__ MoverQueue<R> queues[kWarps];
   MoverQueue<R>& Q = queues[threadIdx.x >> 5];
@@ -546,11 +547,11 @@ push_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ inter
     PState<R> nxt;
     load_state<R, VL>(part + (size_t)next * kChunk, lc.lane_off, lc.lane_cell_off,
                       next < nchunks && next * 32 + lc.lane < n, nxt);
-    push_chunk<R, VL, LITERAL, FAST, false>(part, n, chunk, cur, interp, acc, a, status, Q, qn, lc,
+    push_chunk<R, VL, LITERAL, FAST, false, Acc>(part, n, chunk, cur, interp, acc, a, status, Q, qn, lc,
                                             nullptr, nowin, 0, 0);
     cur = nxt;
   }
-  drain_queue<R, VL, FAST>(part, Q, qn, lc.lane, a, acc, status);
+  drain_queue<R, VL, FAST, Acc>(part, Q, qn, lc.lane, a, acc, status);
 }
 
 // ------------------------------------------------------------ tiled kernel
@@ -673,10 +674,10 @@ __device__ __forceinline__ int tile_sample(const unsigned char* __restrict__ par
 // their chunks of tile j gathering from the window, and arrive on
 // empty[j % 2].  No CTA-wide barrier: a warp delayed by a queue drain holds up
 // nobody until the producer needs its buffer again.
-template <class R, int VL, bool LITERAL, bool FAST>
+template <class R, int VL, bool LITERAL, bool FAST, class Acc>
 __global__ void __launch_bounds__(kTiledThreads, sizeof(R) == 4 ? 2 : 1)  // FP32: 64 registers
 push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
-                  R* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status,
+                  Acc* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status,
                   int chunks_per_warp, int wxmax) {
   constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -753,7 +754,7 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
       load_state<R, VL>(part + (size_t)next * kChunk, lc.lane_off, lc.lane_cell_off,
                         (!last || t1 < ntiles) && next < nchunks && next * 32 + lc.lane < n, nxt);
       if (chunk < nchunks)
-        push_chunk<R, VL, LITERAL, FAST, true>(part, n, chunk, cur, interp, acc, a, status, Q, qn,
+        push_chunk<R, VL, LITERAL, FAST, true, Acc>(part, n, chunk, cur, interp, acc, a, status, Q, qn,
                                                lc, wb, w, ys, zs);
       cur = nxt;
     }
@@ -761,14 +762,14 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
     if (lc.lane == 0) mbar_arrive(&empty[b]);
   }
   if (!ok && lc.lane == 0) atomicOr(status, CPIC_STATUS_PIPELINE);
-  drain_queue<R, VL, FAST>(part, Q, qn, lc.lane, a, acc, status);
+  drain_queue<R, VL, FAST, Acc>(part, Q, qn, lc.lane, a, acc, status);
 }
 
 // ------------------------------------------------------------ host side
-template <class R, int VL, bool LITERAL, bool FAST>
+template <class R, int VL, bool LITERAL, bool FAST, class Acc>
 int launch_push(void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
                 int* status, cudaStream_t s) {
-  auto kern = push_kernel<R, VL, LITERAL, FAST>;
+  auto kern = push_kernel<R, VL, LITERAL, FAST, Acc>;
   static int per_sm[64] = {0};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CPIC_ECUDA;
@@ -783,7 +784,7 @@ int launch_push(void* particles, int n, const void* interp, void* acc, const Pus
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, kPushThreads, 0, s>>>(static_cast<unsigned char*>(particles), n,
-                                                static_cast<const R*>(interp), static_cast<R*>(acc), a,
+                                                static_cast<const R*>(interp), static_cast<Acc*>(acc), a,
                                                 status);
   return launch_status();
 }
@@ -809,10 +810,10 @@ inline TileShape tile_shape(const GridDev& g) {
   return ts;
 }
 
-template <class R, int VL, bool LITERAL, bool FAST>
+template <class R, int VL, bool LITERAL, bool FAST, class Acc>
 int launch_push_tiled(void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
                       int* status, cudaStream_t s) {
-  auto kern = push_tiled_kernel<R, VL, LITERAL, FAST>;
+  auto kern = push_tiled_kernel<R, VL, LITERAL, FAST, Acc>;
   const TileShape ts = tile_shape(a.g);
   const size_t dyn = tiled_dyn_smem<R>(ts.wxmax);
   static size_t opted[64] = {0};
@@ -838,16 +839,16 @@ int launch_push_tiled(void* particles, int n, const void* interp, void* acc, con
   if (blocks > ntiles) blocks = ntiles;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, kTiledThreads, dyn, s>>>(static_cast<unsigned char*>(particles), n,
-                                                  static_cast<const R*>(interp), static_cast<R*>(acc), a,
+                                                  static_cast<const R*>(interp), static_cast<Acc*>(acc), a,
                                                   status, ts.chunks_per_warp, ts.wxmax);
   return launch_status();
 }
 
-template <class R, int VL, bool LITERAL, bool FAST>
+template <class R, int VL, bool LITERAL, bool FAST, class Acc = R>
 int launch_any(bool tiled, void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
                int* status, cudaStream_t s) {
-  return tiled ? launch_push_tiled<R, VL, LITERAL, FAST>(particles, n, interp, acc, a, status, s)
-               : launch_push<R, VL, LITERAL, FAST>(particles, n, interp, acc, a, status, s);
+  return tiled ? launch_push_tiled<R, VL, LITERAL, FAST, Acc>(particles, n, interp, acc, a, status, s)
+               : launch_push<R, VL, LITERAL, FAST, Acc>(particles, n, interp, acc, a, status, s);
 }
 
 // Dispatch over real_t, vector length, the sqrt variant and the kernel.
@@ -861,6 +862,10 @@ int push_dispatch(void* particles, int n, const void* interp, void* acc, const c
   if (prm->precision == CPIC_FLOAT) {
     PushArgs<float> a{(float)prm->qdt_2mc, (float)prm->cdt_dx, (float)prm->cdt_dy,
                       (float)prm->cdt_dz, (float)prm->qsp, gd};
+    if (prm->flags & CPIC_PUSH_ACC_F64)  // FP32 particles, FP64 accumulator rows
+      return prm->particle_vl == 32
+                 ? launch_any<float, 32, true, FAST, double>(tiled, particles, n, interp, acc, a, status, s)
+                 : launch_any<float, 16, true, FAST, double>(tiled, particles, n, interp, acc, a, status, s);
     return prm->particle_vl == 32 ? launch_any<float, 32, true, FAST>(tiled, particles, n, interp, acc, a, status, s)
                                   : launch_any<float, 16, true, FAST>(tiled, particles, n, interp, acc, a, status, s);
   }

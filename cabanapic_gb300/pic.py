@@ -84,11 +84,13 @@ def push(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy
     selects the streaming kernel (no shared-memory cell windows; same
     results, slower once particles are in cell order)."""
     lib = capi.load()
+    # an FP64 accumulator with FP32 particles: the compensated per-cell current sum
+    acc_f64 = particles.precision == capi.CPIC_FLOAT and a0.precision == capi.CPIC_DOUBLE
     flags = ((capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0) | (capi.CPIC_PUSH_EXACT if exact else 0)
-             | (0 if tiles else capi.CPIC_PUSH_STREAMING))
+             | (0 if tiles else capi.CPIC_PUSH_STREAMING) | (capi.CPIC_PUSH_ACC_F64 if acc_f64 else 0))
     prm = capi.CpicPushParams(float(qdt_2mc), float(cdt_dx), float(cdt_dy), float(cdt_dz),
                               float(qsp), particles.precision, particles.vl, flags, 0)
-    if f0.precision != particles.precision or a0.precision != particles.precision:
+    if f0.precision != particles.precision or (a0.precision != particles.precision and not acc_f64):
         raise capi.CpicError("cpic_push", capi.CPIC_EINVAL, "mixed real_t precisions")
     grid = _grid(nx, ny, nz, num_ghosts, boundary)
     if f0.num_cells < grid_cells(nx, ny, nz, num_ghosts) or a0.num_cells < grid_cells(nx, ny, nz, num_ghosts):
@@ -134,8 +136,13 @@ def clear_accumulator_array(fields: FieldArray, accumulators: AccumulatorArray, 
 
 def unload_accumulator_array(fields: FieldArray, accumulators: AccumulatorArray, nx, ny, nz, ng,
                              dx, dy, dz, dt, *, boundary=Boundary.Periodic, stream=None) -> None:
-    """unload_accumulator_array (src/accumulator.cpp:45-122)."""
-    capi.load().call("cpic_unload_accumulator", fields.ptr, accumulators.ptr,
+    """unload_accumulator_array (src/accumulator.cpp:45-122).  An FP64
+    accumulator with FP32 fields (the compensated current sum of an FP32 push)
+    is unloaded in double and rounded once."""
+    fn = ("cpic_unload_accumulator_f64"
+          if accumulators.precision == capi.CPIC_DOUBLE and fields.precision == capi.CPIC_FLOAT
+          else "cpic_unload_accumulator")
+    capi.load().call(fn, fields.ptr, accumulators.ptr,
                      C.byref(_grid(nx, ny, nz, ng, boundary)), float(dx), float(dy), float(dz),
                      float(dt), fields.precision, _stream(stream))
 

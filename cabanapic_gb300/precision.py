@@ -1,9 +1,10 @@
 """Precision study: FP32 against FP64 on the same seeded thermal plasma.
 
 Runs (a) the FP32 path (FP32 push, deposit and field stencils; FP64 energy
-and charge reductions) and (b) the full-FP64 GPU build from the same initial
-state (drawn in FP64; (a) starts from it rounded to FP32), and reports per
-step:
+and charge reductions), (a') the same with FP64 accumulator rows (the
+compensated per-cell current sum) and (b) the full-FP64 GPU build from the
+same initial state (drawn in FP64; (a) starts from it rounded to FP32), and
+reports per step:
   * field L2 relative error of (a) against (b): ||F_a - F_b|| / ||F_b|| over
     E and cB on the interior,
   * total-energy drift of each run: field energy (0.5 sum (E^2 + cB^2) dV,
@@ -84,10 +85,12 @@ def run(cells=128, ppc=32, steps=1000, seed=2024, sample_every=1, sort_interval=
     host32 = {k: (v.astype(np.float32) if k != "cell" else v) for k, v in host64.items()}
     host32["w"] = np.full(len(host32["w"]), deck32.derived()["we"], np.float32)
     sims = {"fp32": Simulation(deck32, host32, sort_interval=sort_interval, max_steps=steps),
+            "fp32_acc64": Simulation(deck32, host32, sort_interval=sort_interval, max_steps=steps,
+                                     acc_f64=True),
             "fp64": Simulation(deck64, host64, sort_interval=sort_interval, max_steps=steps)}
     trk = {k: _Tracker(s) for k, s in sims.items()}
     rows = []
-    times = {"fp32": 0.0, "fp64": 0.0}
+    times = {k: 0.0 for k in sims}
     for step in range(1, steps + 1):
         for k, s in sims.items():
             torch.cuda.synchronize()
@@ -109,6 +112,8 @@ def run(cells=128, ppc=32, steps=1000, seed=2024, sample_every=1, sort_interval=
     w32 = sims["fp32"].energies().sum(axis=1)
     w64 = sims["fp64"].energies().sum(axis=1)
     werr = np.abs(w32 - w64) / np.where(w64 > 0, w64, 1.0)
+    w3264 = sims["fp32_acc64"].energies().sum(axis=1)
+    werr_acc64 = np.abs(w3264 - w64) / np.where(w64 > 0, w64, 1.0)
     half = slice(len(w64) // 2, None)
     level = abs(float(w32[half].mean()) - float(w64[half].mean())) / float(w64[half].mean())
     first_1e4 = next((i + 1 for i, e in enumerate(werr) if e > 1e-4), None)
@@ -120,6 +125,8 @@ def run(cells=128, ppc=32, steps=1000, seed=2024, sample_every=1, sort_interval=
         "fp32_over_fp64": times["fp64"] / times["fp32"],
         "max_field_l2_rel": max(r["field_l2_rel"] for r in rows),
         "field_energy_rel_err_max": float(werr.max()),
+        "field_energy_rel_err_max_fp32_acc64": float(werr_acc64.max()),
+        "pushes_per_s_fp32_acc64": n * steps / times["fp32_acc64"],
         "field_energy_rel_err_final": float(werr[-1]),
         "field_energy_first_step_above_1e-4": first_1e4,
         "field_energy_level_rel_diff_second_half": level,

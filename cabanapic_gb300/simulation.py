@@ -23,7 +23,8 @@ from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleLis
 class Simulation:
     def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
                  max_steps: int = None, time_push: bool = False, exact: bool = False,
-                 tiles: bool = True, fields=None, particle_dump=None, field_dump=None):
+                 tiles: bool = True, fields=None, particle_dump=None, field_dump=None,
+                 acc_f64: bool = False):
         self.deck = deck
         self.p = deck.derived()
         dev = torch.device(device if device is not None else "cuda")
@@ -32,7 +33,8 @@ class Simulation:
         nc = deck.num_cells
         self.particles = ParticleList(deck.num_particles, R, deck.vl, dev)
         self.interpolators = InterpolatorArray(nc, R, dev)
-        self.accumulators = AccumulatorArray(nc, R, dev)
+        # acc_f64 (FP32 decks): FP64 accumulator rows, the compensated per-cell current sum
+        self.accumulators = AccumulatorArray(nc, np.float64 if acc_f64 else R, dev)
         self.fields = FieldArray(nc, R, dev)
         self.solver = pic.EMFieldSolver(self.fields, deck.boundary)
         pic.initialize_interpolator(self.interpolators)

@@ -65,6 +65,12 @@ typedef struct CUstream_st* cpic_stream_t;
                                   shared-memory cell window.  Same results as the default
                                   tiled kernel, which is faster once particles are in cell
                                   order. */
+#define CPIC_PUSH_ACC_F64 8    /* real_t = float only: `accumulators` holds double rows
+                                  ([cell][3][4] of double, 96 B per cell).  Warps still
+                                  reduce their deposits in float; the sum over warps, streaks
+                                  and particles (the per-cell current sum, k terms at k
+                                  particles per cell) runs in double, so its error no longer
+                                  grows with k.  Unload with cpic_unload_accumulator_f64. */
 
 /* Grid of the run: interior cells nx*ny*nz plus num_ghosts ghost layers;
  * boundary is the deck's BOUNDARY_TYPE, which the reference's field code reads
@@ -129,6 +135,13 @@ int cpic_clear_accumulator(void* accumulators, int64_t num_cells, int32_t precis
 int cpic_unload_accumulator(void* fields, const void* accumulators, const cpic_grid* grid,
                             double dx, double dy, double dz, double dt, int32_t precision,
                             cpic_stream_t stream);
+
+/* unload_accumulator_array from the double accumulator rows of a push with
+ * CPIC_PUSH_ACC_F64: the four-term sums and the scaling run in double, jf is
+ * rounded once to the fields' real_t (precision). */
+int cpic_unload_accumulator_f64(void* fields, const double* accumulators, const cpic_grid* grid,
+                                double dx, double dy, double dz, double dt, int32_t precision,
+                                cpic_stream_t stream);
 
 /* Replaces: Field_Solver<EM_Field_Solver>::advance_b(field_array_t&, real_t px, py, pz,
  *   size_t nx, ny, nz, ng)                     -- src/fields.h:352-364, 668-719

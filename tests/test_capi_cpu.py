@@ -66,7 +66,7 @@ def test_push_argument_validation(lib):
     assert push(dummy, 10, dummy, dummy, C.byref(g), None, C.byref(status), None) == capi.CPIC_EINVAL
     assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(precision=2)), C.byref(status), None) == capi.CPIC_EINVAL
     assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(particle_vl=8)), C.byref(status), None) == capi.CPIC_EINVAL
-    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(flags=8)), C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(flags=16)), C.byref(status), None) == capi.CPIC_EINVAL
     assert push(None, 10, dummy, dummy, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
     assert push(dummy, -1, dummy, dummy, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
     # empty particle list: nothing to do, no device access

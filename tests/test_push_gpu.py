@@ -156,3 +156,52 @@ def test_fast_and_exact_agree_on_a_thermal_plasma(orc):
              p["cdt_dz"], p["qsp"], acc, orc.grid(12, 12, 12))
     assert np.array_equal(out[True][0], ref)
     assert_particles_close(out[False][0], ref, deck.num_particles, np.float32, 32, 12, 12, 12)
+
+
+@pytest.mark.parametrize("tiles", [True, False])
+def test_fp64_accumulation_bounds_hot_cell_error(orc, tiles):
+    """CPIC_PUSH_ACC_F64: 8192 FP32 particles deposit into one cell.  The truth
+    is the exact sum (math.fsum) of each particle's 12 FP32 deposits, taken
+    from the oracle one particle at a time (the exact variant computes the
+    same per-particle values).  With FP64 accumulator rows the GPU's error is
+    the warps' FP32 tree alone (5 levels of 32 lanes), independent of the
+    number of particles: at most 4 eps32 sum|x| per element."""
+    import math
+    from cabanapic_gb300 import layout as L, pic
+    st = random_state(nx=4, ny=4, nz=4, n=8192, seed=17, crossing=0.0, edge_cases=False)
+    R = np.float32
+    h = {k: v.copy() for k, v in st["host"].items()}
+    h["cell"][:] = L.voxel(2, 3, 2, 4, 4)
+    rng = np.random.default_rng(3)
+    for k in ("x", "y", "z"):
+        h[k] = rng.uniform(-0.8, 0.8, 8192).astype(R)
+    for k in ("ux", "uy", "uz"):
+        h[k] = (rng.standard_normal(8192) * 0.05).astype(R)
+    nc = st["num_cells"]
+    cell = int(h["cell"][0])
+    per = np.zeros((8192, 12))
+    for i in range(8192):
+        one = {k: v[i:i + 1] for k, v in h.items()}
+        acc1 = np.zeros((nc, 3, 4), R)
+        assert orc.push(L.pack_particles(one, R, 32), 1, 32, st["interp"], *st["push_args"], acc1, st["ogrid"]) == 0
+        per[i] = acc1[cell].reshape(12)
+    truth = np.array([math.fsum(per[:, k]) for k in range(12)])
+    absum = np.abs(per).sum(axis=0)
+    P = pic.ParticleList(8192, R, 32).upload(h)
+    I = pic.InterpolatorArray(nc, R)
+    I.buf.copy_(torch.from_numpy(st["interp"]))
+    A64 = pic.AccumulatorArray(nc, np.float64)
+    pic.push(P, I, *st["push_args"], A64, None, 4, 4, 4, 1, pic.Boundary.Periodic, exact=True, tiles=tiles)
+    pic.check_status()
+    got = A64.get()[cell].reshape(12)
+    eps = np.finfo(np.float32).eps
+    assert np.all(np.abs(got - truth) <= 4 * eps * absum), (np.abs(got - truth) / (eps * absum)).max()
+    # the FP32 accumulator sums the same warp totals in float; record its error for comparison
+    P32 = pic.ParticleList(8192, R, 32).upload(h)
+    A32 = pic.AccumulatorArray(nc, R)
+    pic.push(P32, I, *st["push_args"], A32, None, 4, 4, 4, 1, pic.Boundary.Periodic, exact=True, tiles=tiles)
+    pic.check_status()
+    err32 = np.abs(A32.get()[cell].reshape(12).astype(np.float64) - truth) / (eps * absum)
+    assert np.all(err32 <= 2 * 8192 / 32)  # the recursive-summation bound over the warp totals
+    # the particle states are the same as with FP32 accumulators
+    assert np.array_equal(P.download_bytes(), P32.download_bytes())
