@@ -204,6 +204,34 @@ struct EnergyScratch {
   unsigned int done;
 };
 
+// Sum of squares per thread.  FP32: each square is split exactly into
+// p + q (p = a*a rounded, q = fma(a, a, -p)), the p are summed in float-float
+// (two-sum: the rounding error of every addition is kept in `lo`) and the q in
+// `lo`; the thread's total hi + lo goes to the FP64 reduction.  Relative
+// accuracy ~1e-14, without FP64 arithmetic per cell (slow on GB300's FP64
+// pipe).  FP64: plain double sums.
+template <class R>
+struct SqAcc {
+  double s = 0.0;
+  __device__ __forceinline__ void add(R a) { s += (double)a * (double)a; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct SqAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float a) {
+    const float p = __fmul_rn(a, a);
+    const float q = __fmaf_rn(a, a, -p);
+    const float t = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(t, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    hi = t;
+    lo = __fadd_rn(lo, __fadd_rn(err, q));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 template <class R>
 __global__ void __launch_bounds__(kThreads)
 energy_kernel(const R* __restrict__ F, const GridDev g, double* __restrict__ out,
@@ -215,18 +243,17 @@ energy_kernel(const R* __restrict__ F, const GridDev g, double* __restrict__ out
   const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
   const int lane = threadIdx.x & 31;
-  double e = 0.0, bb = 0.0;
+  SqAcc<R> ea, ba;
   for (unsigned r = warp; r < rows; r += nwarps) {
     const int y = (int)(r % (unsigned)g.ny) + 1, z = (int)(r / (unsigned)g.ny) + 1;
     const int row = g.vox(0, y, z);
     for (int x = 1 + lane; x <= g.nx; x += 32) {
       const int i = row + x;
-      const double a0 = F[cell_at<9>(i, CPIC_F_EX)], a1 = F[cell_at<9>(i, CPIC_F_EY)], a2 = F[cell_at<9>(i, CPIC_F_EZ)];
-      const double c0 = F[cell_at<9>(i, CPIC_F_CBX)], c1 = F[cell_at<9>(i, CPIC_F_CBY)], c2 = F[cell_at<9>(i, CPIC_F_CBZ)];
-      e += a0 * a0 + a1 * a1 + a2 * a2;
-      bb += c0 * c0 + c1 * c1 + c2 * c2;
+      ea.add(F[cell_at<9>(i, CPIC_F_EX)]); ea.add(F[cell_at<9>(i, CPIC_F_EY)]); ea.add(F[cell_at<9>(i, CPIC_F_EZ)]);
+      ba.add(F[cell_at<9>(i, CPIC_F_CBX)]); ba.add(F[cell_at<9>(i, CPIC_F_CBY)]); ba.add(F[cell_at<9>(i, CPIC_F_CBZ)]);
     }
   }
+  double e = ea.value(), bb = ba.value();
   for (int o = 16; o > 0; o >>= 1) {
     e += __shfl_xor_sync(kFull, e, o);
     bb += __shfl_xor_sync(kFull, bb, o);
