@@ -203,9 +203,10 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
 
 def e2e_run(precision, steps, warmup, host_packed, ws):
     """Same step loop through the public API, with host buffers: the initial
-    particle state is copied from pinned host memory, each step's energies are
-    read back to pinned host memory, and the final particle state is copied
-    back, all inside the timed region."""
+    particle state is copied from pinned host memory (ParticleList.upload_pinned:
+    8 concurrent copies), each step's energies are read back to pinned host
+    memory, and the final particle state is copied back
+    (ParticleList.download_pinned), all inside the timed region."""
     import torch
     from cabanapic_gb300 import decks, pic
     from cabanapic_gb300.simulation import Simulation
@@ -225,12 +226,12 @@ def e2e_run(precision, steps, warmup, host_packed, ws):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    sim.particles.buf[: sim.particles.nbytes].copy_(pinned_in, non_blocking=True)
+    sim.particles.upload_pinned(pinned_in)
     sim.fields.buf.zero_()
     for k in range(steps):
         sim.step()
         energies_host[k].copy_(sim.energy[k], non_blocking=True)
-    pinned_out.copy_(sim.particles.buf[: sim.particles.nbytes], non_blocking=True)
+    sim.particles.download_pinned(pinned_out)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)

@@ -22,6 +22,40 @@ def _torch_real(real: np.dtype):
     return torch.float32 if np.dtype(real) == np.float32 else torch.float64
 
 
+_COPY_STREAMS = {}
+
+
+def copy_in_pieces(dst: torch.Tensor, src: torch.Tensor, pieces: int = 8) -> None:
+    """dst.copy_(src) between pinned host and device memory as `pieces`
+    asynchronous copies on side streams, so that several copy engines move
+    the bytes at once.  Ordered after the current stream's earlier work; the
+    current stream waits for all pieces.  One cudaMemcpyAsync per piece."""
+    assert dst.numel() == src.numel() and dst.dtype == src.dtype
+    dev = dst.device if dst.is_cuda else src.device
+    cur = torch.cuda.current_stream(dev)
+    streams = _COPY_STREAMS.get(dev)
+    if streams is None or len(streams) < pieces:
+        streams = [torch.cuda.Stream(dev) for _ in range(pieces)]
+        _COPY_STREAMS[dev] = streams
+    n = dst.numel()
+    step = -(-n // pieces)
+    start = torch.cuda.Event()
+    start.record(cur)
+    dev_t = dst if dst.is_cuda else src
+    for i in range(pieces):
+        a, b = i * step, min(n, (i + 1) * step)
+        if a >= b:
+            break
+        s = streams[i]
+        s.wait_event(start)
+        with torch.cuda.stream(s):
+            dst[a:b].copy_(src[a:b], non_blocking=True)
+        dev_t.record_stream(s)
+        done = torch.cuda.Event()
+        done.record(s)
+        cur.wait_event(done)
+
+
 class ParticleList:
     """particle_list_t: Cabana AoSoA<real_t x7, int> of n particles."""
 
@@ -49,6 +83,18 @@ class ParticleList:
         assert packed.nbytes == self.nbytes, (packed.nbytes, self.nbytes)
         self.buf[: self.nbytes].copy_(torch.from_numpy(packed.view(np.uint8)))
         return self
+
+    def upload_pinned(self, pinned: torch.Tensor, pieces: int = 8) -> "ParticleList":
+        """Asynchronous upload of packed AoSoA bytes from a pinned host tensor
+        (uint8, nbytes), split over several copy engines; stream-ordered."""
+        copy_in_pieces(self.buf[: self.nbytes], pinned, pieces)
+        return self
+
+    def download_pinned(self, pinned: torch.Tensor, pieces: int = 8) -> torch.Tensor:
+        """Asynchronous download of the AoSoA bytes into a pinned host tensor;
+        complete once the current stream has reached this point."""
+        copy_in_pieces(pinned, self.buf[: self.nbytes], pieces)
+        return pinned
 
     def download_bytes(self) -> np.ndarray:
         return self.buf[: self.nbytes].cpu().numpy()
