@@ -195,7 +195,9 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     ms = e0.elapsed_time(e1)
     push_ms = sim.push_times_ms()
     sim.check_status()
-    res = dict(ms=ms, push_ms=push_ms, deck=deck, energies=sim.energies())
+    # timed steps that sorted first (step numbers count the warm-up steps)
+    sort_steps = [k for k in range(steps) if (warmup + k) % SORT_INTERVAL == 0]
+    res = dict(ms=ms, push_ms=push_ms, deck=deck, energies=sim.energies(), sort_steps=sort_steps)
     del sim
     torch.cuda.empty_cache()
     return res, host_packed
@@ -374,7 +376,8 @@ def main():
         return
     traffic = _traffic_from_profiles()
     per_step_launches = 11  # interp, push, unload, 2x(advance_b + ghost copy), fold, ghost copy, advance_e, energies
-    launches = args.steps * per_step_launches + 6 * len(range(0, args.steps, SORT_INTERVAL))
+    # a sort adds rank, 3 scan passes, scatter and gather
+    launches = args.steps * per_step_launches + 6 * len(res["sort_steps"])
 
     exact = None
     if not args.no_exact:
