@@ -3,7 +3,8 @@
 Workload (the reference's throughput configuration): uniform thermal plasma,
 128^3 periodic cells, 64 electrons per cell (134,217,728 particles), FP32,
 u_th = 0.05, dt = 0.7 Courant, zero initial fields, particles re-sorted by
-cell every 20 steps.  A "step" is the reference's whole time step
+cell every 14 steps (the measured optimum of sort cost against the push's
+growing cost as particles drift out of cell order).  A "step" is the reference's whole time step
 (example/example.cpp:221-271): interpolator load, accumulator clear, push with
 deposit, accumulator unload, B half step, E step, B half step, field energies,
 plus the amortised sort.  The particle list (4.3 GB) is larger than L2, so no
@@ -35,7 +36,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SORT_INTERVAL = 20
+SORT_INTERVAL = 14
 N_CELLS = 128
 PPC = 64
 TILES = True
@@ -314,7 +315,7 @@ def main():
     metric = "particle-pushes/s (full step, FP32)"
     unit = "particle-pushes/s"
     workload = (f"thermal plasma {N_CELLS}^3 cells x {PPC} ppc = {N_CELLS ** 3 * PPC:,} particles, "
-                "FP32, u_th=0.05, dt=0.7 Courant, sort every 20 steps; full step (interp, clear, "
+                f"FP32, u_th=0.05, dt=0.7 Courant, sort every {SORT_INTERVAL} steps; full step (interp, clear, "
                 "push+deposit, unload, advance_b/e/b, energies)")
 
     if args.impl == "reference":
@@ -365,7 +366,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "diocotron column 96x96x64 cells, annulus 0.20<r/R<0.35 at 128 "
                                        "particles per cell of annulus volume, cB_z = 5, E x B loading "
-                                       "from the t=0 Poisson field, dt=0.99 Courant, sort every 20 steps",
+                                       f"from the t=0 Poisson field, dt=0.99 Courant, sort every {SORT_INTERVAL} steps",
                            "particles": n, "cells": deck.num_cells,
                            "push_kernel": "tiled" if TILES else "streaming"},
                 "push_ms": push_ms, "push_ms_by_step": [round(t, 4) for t in res["push_ms"]],

@@ -7,12 +7,15 @@
 //
 // Passes (keys are cell indices in [0, num_cells); an out-of-range key sorts
 // after all valid ones):
-//   1. rank:    per particle, its arrival rank in its cell (warp-aggregated
-//               atomics: one atomic per distinct cell per warp)
-//   2. scan:    exclusive prefix sum of the per-cell counts -> cell offsets
-//   3. scatter: perm[offset[cell] + rank] = particle index
+//   1. count:   per-cell particle counts (reductions, no return values)
+//   2. scan:    exclusive prefix sum of the counts -> cell offsets
+//   3. scatter: each particle takes the next slot of its cell from the offset
+//               (atomics with return) and writes perm[slot] = its index
 //   4. gather:  particles[d] = copy[perm[d]], member by member (coalesced writes)
-// The order within a cell depends on atomic arrival order.  The in-place
+// Passes 1 and 3 aggregate over the lanes of a warp that share a cell: one
+// atomic per cell per 32 particles.  Each warp takes kSortChunks chunks of 32 particles, all
+// loads and atomics issued before their results are used.  The order within
+// a cell depends on atomic arrival order.  The in-place
 // entry point gathers from a copy of the list in the scratch; the
 // out-of-place one (for callers with two lists) gathers straight into the
 // second list and skips that copy.
@@ -23,6 +26,7 @@
 namespace cpic {
 
 constexpr int kSortThreads = 256;
+constexpr int kSortChunks = 4;  // 32-particle chunks per warp in the count and scatter passes
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -30,7 +34,7 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct SortPlan {
-  size_t counts_off, sums_off, rank_off, perm_off, copy_off, total;
+  size_t counts_off, sums_off, perm_off, copy_off, total;
   int64_t nkeys, nscan_blocks;
 };
 
@@ -41,32 +45,63 @@ static SortPlan plan_sort(int64_t n, int64_t num_cells, int prec, int vl) {
   size_t off = 0;
   p.counts_off = off; off += align256(sizeof(int) * (size_t)p.nkeys);
   p.sums_off = off;   off += align256(sizeof(int) * (size_t)p.nscan_blocks);
-  p.rank_off = off;   off += align256(sizeof(int) * (size_t)n);
   p.perm_off = off;   off += align256(sizeof(int) * (size_t)n);
   p.copy_off = off;   off += align256(cpic_particle_list_bytes(n, prec, vl));
   p.total = off;
   return p;
 }
 
+// Cell key of particle p: out-of-range cells go to the last bucket; lanes
+// past the end get distinct negative keys.
+template <class R, int VL>
+__device__ __forceinline__ int sort_key(const unsigned char* __restrict__ part, int64_t p, int n,
+                                        int num_cells, int lane) {
+  using L = PLayout<R, VL>;
+  if (p >= n) return -1 - lane;
+  const int c = __ldg(reinterpret_cast<const int*>(part + L::cell_off(p)));
+  return ((unsigned)c < (unsigned)num_cells) ? c : num_cells;
+}
+
+// Groups of equal keys among the warp's lanes: `leader` is the group's first
+// lane, `len` its size and `rank` this lane's place in it.  A chunk made of
+// one or two runs of equal keys (most chunks of a sorted list) takes a
+// shuffle-and-ballot run test; others group with __match_any_sync, which
+// keeps one atomic per distinct cell when strays split a cell's run.
+__device__ __forceinline__ void key_group(int key, int lane, int& leader, int& len, int& rank) {
+  const int left = __shfl_up_sync(kFull, key, 1);
+  const unsigned heads = __ballot_sync(kFull, lane == 0 || key != left);
+  if (__popc(heads) <= 2) {  // warp-uniform
+    const unsigned upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
+    leader = 31 - __clz(heads & upto);
+    const unsigned above = heads & ~upto;
+    len = (above ? __ffs(above) - 1 : 32) - leader;
+    rank = lane - leader;
+  } else {
+    const unsigned peers = __match_any_sync(kFull, key);
+    leader = __ffs(peers) - 1;
+    len = __popc(peers);
+    rank = __popc(peers & ((1u << lane) - 1u));
+  }
+}
+
+__device__ __forceinline__ int64_t sort_chunk0() {
+  return ((int64_t)blockIdx.x * (kSortThreads / 32) + (threadIdx.x >> 5)) * kSortChunks;
+}
+
 template <class R, int VL>
 __global__ void __launch_bounds__(kSortThreads)
-rank_kernel(const unsigned char* __restrict__ part, int n, int num_cells, int* __restrict__ counts,
-            int* __restrict__ rank) {
-  using L = PLayout<R, VL>;
+count_kernel(const unsigned char* __restrict__ part, int n, int num_cells, int* __restrict__ counts) {
   const int lane = lane_id();
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = p < n;
-  int key = -1 - lane;
-  if (valid) {
-    int c = __ldg(reinterpret_cast<const int*>(part + L::cell_off(p)));
-    key = ((unsigned)c < (unsigned)num_cells) ? c : num_cells;
+  const int64_t c0 = sort_chunk0();
+  int key[kSortChunks];
+#pragma unroll
+  for (int k = 0; k < kSortChunks; ++k) key[k] = sort_key<R, VL>(part, (c0 + k) * 32 + lane, n, num_cells, lane);
+#pragma unroll
+  for (int k = 0; k < kSortChunks; ++k) {
+    int leader, len, rank;
+    key_group(key[k], lane, leader, len, rank);
+    if (leader == lane && key[k] >= 0) atomicAdd(counts + key[k], len);
   }
-  const unsigned peers = __match_any_sync(kFull, key);
-  const int leader = __ffs(peers) - 1;
-  int base = 0;
-  if (valid && lane == leader) base = atomicAdd(counts + key, __popc(peers));
-  base = __shfl_sync(kFull, base, leader);
-  if (valid) rank[p] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 // Block-local exclusive scan of kScanTile ints; returns the tile total.
@@ -146,16 +181,29 @@ scan_add_kernel(int* __restrict__ data, int64_t n, const int* __restrict__ sums)
   }
 }
 
+// cursor: the cell offsets, advanced as slots are taken.
 template <class R, int VL>
 __global__ void __launch_bounds__(kSortThreads)
-scatter_kernel(const unsigned char* __restrict__ part, int n, int num_cells,
-               const int* __restrict__ offsets, const int* __restrict__ rank, int* __restrict__ perm) {
-  using L = PLayout<R, VL>;
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  int c = __ldg(reinterpret_cast<const int*>(part + L::cell_off(p)));
-  c = ((unsigned)c < (unsigned)num_cells) ? c : num_cells;
-  perm[offsets[c] + rank[p]] = (int)p;
+scatter_kernel(const unsigned char* __restrict__ part, int n, int num_cells, int* __restrict__ cursor,
+               int* __restrict__ perm) {
+  const int lane = lane_id();
+  const int64_t c0 = sort_chunk0();
+  int key[kSortChunks], leader[kSortChunks], rank[kSortChunks], base[kSortChunks];
+#pragma unroll
+  for (int k = 0; k < kSortChunks; ++k) key[k] = sort_key<R, VL>(part, (c0 + k) * 32 + lane, n, num_cells, lane);
+#pragma unroll
+  for (int k = 0; k < kSortChunks; ++k) {
+    int len;
+    key_group(key[k], lane, leader[k], len, rank[k]);
+    base[k] = 0;
+    if (leader[k] == lane && key[k] >= 0) base[k] = atomicAdd(cursor + key[k], len);
+  }
+#pragma unroll
+  for (int k = 0; k < kSortChunks; ++k) {
+    const int b = __shfl_sync(kFull, base[k], leader[k]);
+    const int64_t p = (c0 + k) * 32 + lane;
+    if (p < n) perm[b + rank[k]] = (int)p;
+  }
 }
 
 template <class R, int VL>
@@ -179,17 +227,18 @@ static int sort_typed(void* particles, void* dst, int n, int num_cells, const So
                       unsigned char* sc, cudaStream_t s) {
   int* counts = reinterpret_cast<int*>(sc + pl.counts_off);
   int* sums = reinterpret_cast<int*>(sc + pl.sums_off);
-  int* rank = reinterpret_cast<int*>(sc + pl.rank_off);
   int* perm = reinterpret_cast<int*>(sc + pl.perm_off);
   unsigned char* copy = sc + pl.copy_off;
   unsigned char* part = static_cast<unsigned char*>(particles);
   const unsigned pb = (unsigned)(((int64_t)n + kSortThreads - 1) / kSortThreads);
+  const int64_t warps = ((int64_t)n + 32 * kSortChunks - 1) / (32 * kSortChunks);
+  const unsigned cb = (unsigned)((warps + kSortThreads / 32 - 1) / (kSortThreads / 32));
   if (cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)pl.nkeys, s) != cudaSuccess) return CPIC_ECUDA;
-  rank_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, n, num_cells, counts, rank);
+  count_kernel<R, VL><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts);
   scan_tiles_kernel<<<(unsigned)pl.nscan_blocks, kScanThreads, 0, s>>>(counts, pl.nkeys, sums);
   scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, pl.nscan_blocks);
   scan_add_kernel<<<(unsigned)pl.nscan_blocks, kScanThreads, 0, s>>>(counts, pl.nkeys, sums);
-  scatter_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, n, num_cells, counts, rank, perm);
+  scatter_kernel<R, VL><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts, perm);
   if (dst) {
     gather_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, static_cast<unsigned char*>(dst), n, perm);
     return launch_status();

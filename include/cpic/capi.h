@@ -236,7 +236,7 @@ int cpic_sort_particles(void* particles, int64_t num_particles, int64_t num_cell
 /* Out-of-place variant for callers that own two particle lists: the same
  * order, gathered from `particles` (unchanged) into `sorted` (distinct, same
  * size), without the in-place variant's copy of the list.  Scratch: the
- * counts, ranks and permutation only (cpic_sort_into_scratch_bytes). */
+ * counts and permutation only (cpic_sort_into_scratch_bytes). */
 size_t cpic_sort_into_scratch_bytes(int64_t num_particles, int64_t num_cells, int32_t precision,
                                     int32_t particle_vl);
 int cpic_sort_particles_into(const void* particles, void* sorted, int64_t num_particles,

@@ -99,7 +99,7 @@ def test_sort_scratch_query(lib):
     from cabanapic_gb300 import layout as L
     n, nc = 100000, 5000
     b = q(n, nc, 4, 32)
-    assert b >= L.particle_list_bytes(n, np.float32, 32) + 8 * n + 4 * nc
+    assert b >= L.particle_list_bytes(n, np.float32, 32) + 4 * n + 4 * nc
     assert q(n, nc, 3, 32) == 0 and q(n, nc, 4, 7) == 0 and q(-1, nc, 4, 32) == 0
 
 
