@@ -27,66 +27,109 @@ inline unsigned blocks_for(int64_t n, int threads = kThreads) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
-// Linear thread index t over an ex*ey*ez box of cells starting at (1,1,1);
-// 32-bit arithmetic (grids are limited to < 2^31 cells).
-__device__ __forceinline__ bool box_coords(unsigned t, unsigned ex, unsigned ey, unsigned ez,
-                                           int& x, int& y, int& z) {
-  if (t >= ex * ey * ez) return false;
-  const unsigned r = t / ex;
-  x = (int)(t - r * ex) + 1;
-  z = (int)(r / ey);
-  y = (int)(r - (unsigned)z * ey) + 1;
-  z += 1;
-  return true;
+// The stencil kernels map each warp to K consecutive 32-cell AoSoA blocks of
+// the linear cell index, so a warp's access to one member is one aligned
+// 128-byte line, and a lane skips a cell outside the kernel's box
+// [1, hx] x [1, hy] x [1, hz].  Each thread issues the loads of all its cells
+// before storing any result.
+struct CellRange {
+  int begin, end;   // linear cells [begin, end); begin is a multiple of 32
+  unsigned blocks;  // launch grid of kThreads-thread blocks
+};
+
+template <int K>
+inline CellRange cell_range(const GridDev& g, int hx, int hy, int hz) {
+  CellRange r;
+  r.begin = g.vox(1, 1, 1) & ~31;
+  r.end = g.vox(hx, hy, hz) + 1;
+  const int64_t warps = ((int64_t)(r.end - r.begin) + 32 * K - 1) / (32 * K);
+  r.blocks = blocks_for(warps * 32);
+  return r;
+}
+
+// This lane's cell in the first of its warp's K blocks (the k-th is 32 k on).
+template <int K>
+__device__ __forceinline__ int lane_cell0(int begin) {
+  const int64_t warp = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  return (int)(begin + warp * (32 * K) + (threadIdx.x & 31));
+}
+
+__device__ __forceinline__ bool cell_in_box(int c, int end, const GridDev& g, int hx, int hy, int hz) {
+  if (c >= end) return false;
+  int y = div_magic(c, g.dsx);
+  const int x = c - y * g.sx;
+  const int z = div_magic(y, g.dsy);
+  y -= z * g.sy;
+  return x >= 1 && x <= hx && y >= 1 && y <= hy && z >= 1 && z <= hz;
 }
 
 // ------------------------------------------------------------ interpolator
 // load_interpolator_array (interpolator.cpp:48-136): interior cells.
 template <class R>
 __global__ void __launch_bounds__(kThreads)
-load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridDev g) {
-  int x, y, z;
-  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx, g.ny, g.nz, x, y, z)) return;
-  const int i = g.vox(x, y, z);
+load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridDev g, int begin, int end) {
+  const int i = lane_cell0<1>(begin);
+  if (!cell_in_box(i, end, g, g.nx, g.ny, g.nz)) return;
   const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
   const R fourth = 1.0 / 4.0, half = 1.0 / 2.0;
+  auto f = [&](int c, int m) { return __ldg(F + cell_at<9>(c, m)); };
+  const R ex0 = f(i, CPIC_F_EX), ex1 = f(i + oy, CPIC_F_EX), ex2 = f(i + oz, CPIC_F_EX),
+          ex3 = f(i + oy + oz, CPIC_F_EX);
+  const R ey0 = f(i, CPIC_F_EY), ey1 = f(i + oz, CPIC_F_EY), ey2 = f(i + ox, CPIC_F_EY),
+          ey3 = f(i + ox + oz, CPIC_F_EY);
+  const R ez0 = f(i, CPIC_F_EZ), ez1 = f(i + ox, CPIC_F_EZ), ez2 = f(i + oy, CPIC_F_EZ),
+          ez3 = f(i + ox + oy, CPIC_F_EZ);
+  const R bx0 = f(i, CPIC_F_CBX), bx1 = f(i + ox, CPIC_F_CBX);
+  const R by0 = f(i, CPIC_F_CBY), by1 = f(i + oy, CPIC_F_CBY);
+  const R bz0 = f(i, CPIC_F_CBZ), bz1 = f(i + oz, CPIC_F_CBZ);
   auto four = [&](int m0, R w0, R w1, R w2, R w3) {
     I[cell_at<18>(i, m0 + 0)] = fourth * ((w3 + w0) + (w1 + w2));
     I[cell_at<18>(i, m0 + 1)] = fourth * ((w3 - w0) + (w1 - w2));
     I[cell_at<18>(i, m0 + 2)] = fourth * ((w3 - w0) - (w1 - w2));
     I[cell_at<18>(i, m0 + 3)] = fourth * ((w3 + w0) - (w1 + w2));
   };
-  four(CPIC_I_EX, F[cell_at<9>(i, CPIC_F_EX)], F[cell_at<9>(i + oy, CPIC_F_EX)],
-       F[cell_at<9>(i + oz, CPIC_F_EX)], F[cell_at<9>(i + oy + oz, CPIC_F_EX)]);
-  four(CPIC_I_EY, F[cell_at<9>(i, CPIC_F_EY)], F[cell_at<9>(i + oz, CPIC_F_EY)],
-       F[cell_at<9>(i + ox, CPIC_F_EY)], F[cell_at<9>(i + ox + oz, CPIC_F_EY)]);
-  four(CPIC_I_EZ, F[cell_at<9>(i, CPIC_F_EZ)], F[cell_at<9>(i + ox, CPIC_F_EZ)],
-       F[cell_at<9>(i + oy, CPIC_F_EZ)], F[cell_at<9>(i + ox + oy, CPIC_F_EZ)]);
-  R w0 = F[cell_at<9>(i, CPIC_F_CBX)], w1 = F[cell_at<9>(i + ox, CPIC_F_CBX)];
-  I[cell_at<18>(i, CPIC_I_CBX)] = half * (w1 + w0);
-  I[cell_at<18>(i, CPIC_I_DCBXDX)] = half * (w1 - w0);
-  w0 = F[cell_at<9>(i, CPIC_F_CBY)]; w1 = F[cell_at<9>(i + oy, CPIC_F_CBY)];
-  I[cell_at<18>(i, CPIC_I_CBY)] = half * (w1 + w0);
-  I[cell_at<18>(i, CPIC_I_DCBYDY)] = half * (w1 - w0);
-  w0 = F[cell_at<9>(i, CPIC_F_CBZ)]; w1 = F[cell_at<9>(i + oz, CPIC_F_CBZ)];
-  I[cell_at<18>(i, CPIC_I_CBZ)] = half * (w1 + w0);
-  I[cell_at<18>(i, CPIC_I_DCBZDZ)] = half * (w1 - w0);
+  four(CPIC_I_EX, ex0, ex1, ex2, ex3);
+  four(CPIC_I_EY, ey0, ey1, ey2, ey3);
+  four(CPIC_I_EZ, ez0, ez1, ez2, ez3);
+  I[cell_at<18>(i, CPIC_I_CBX)] = half * (bx1 + bx0);
+  I[cell_at<18>(i, CPIC_I_DCBXDX)] = half * (bx1 - bx0);
+  I[cell_at<18>(i, CPIC_I_CBY)] = half * (by1 + by0);
+  I[cell_at<18>(i, CPIC_I_DCBYDY)] = half * (by1 - by0);
+  I[cell_at<18>(i, CPIC_I_CBZ)] = half * (bz1 + bz0);
+  I[cell_at<18>(i, CPIC_I_DCBZDZ)] = half * (bz1 - bz0);
 }
 
 // ------------------------------------------------------------ accumulator
 // unload_accumulator_array (accumulator.cpp:71-110): cells [1, n+1] per axis.
 template <class R, class Acc = R>
 __global__ void __launch_bounds__(kThreads)
-unload_kernel(R* __restrict__ F, const Acc* __restrict__ A, const GridDev g, Acc cx, Acc cy, Acc cz) {
-  int x, y, z;
-  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx + 1, g.ny + 1, g.nz + 1, x, y, z)) return;
-  const int i = g.vox(x, y, z);
-  const int xd = g.vox(x - 1, y, z), yd = g.vox(x, y - 1, z), zd = g.vox(x, y, z - 1);
-  const int xzd = g.vox(x - 1, y, z - 1), xyd = g.vox(x - 1, y - 1, z), yzd = g.vox(x, y - 1, z - 1);
+unload_kernel(R* __restrict__ F, const Acc* __restrict__ A, const GridDev g, Acc cx, Acc cy, Acc cz,
+              int begin, int end) {
+  constexpr int K = 2;
+  const int c0 = lane_cell0<K>(begin);
+  const int oy = g.sx, oz = g.sx * g.sy;
   auto a = [&](int c, int k) { return __ldg(A + (size_t)c * 12 + k); };
-  F[cell_at<9>(i, CPIC_F_JFX)] = (R)(cx * (a(i, 0) + a(yd, 1) + a(zd, 2) + a(yzd, 3)));
-  F[cell_at<9>(i, CPIC_F_JFY)] = (R)(cy * (a(i, 4) + a(zd, 5) + a(xd, 6) + a(xzd, 7)));
-  F[cell_at<9>(i, CPIC_F_JFZ)] = (R)(cz * (a(i, 8) + a(xd, 9) + a(yd, 10) + a(xyd, 11)));
+  Acc v[K][12];
+  bool ok[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int i = c0 + 32 * k;
+    ok[k] = cell_in_box(i, end, g, g.nx + 1, g.ny + 1, g.nz + 1);
+    if (ok[k]) {
+      // neighbours x-1, y-1, z-1 and the diagonals (accumulator.cpp:82-107)
+      v[k][0] = a(i, 0); v[k][1] = a(i - oy, 1); v[k][2] = a(i - oz, 2); v[k][3] = a(i - oy - oz, 3);
+      v[k][4] = a(i, 4); v[k][5] = a(i - oz, 5); v[k][6] = a(i - 1, 6); v[k][7] = a(i - 1 - oz, 7);
+      v[k][8] = a(i, 8); v[k][9] = a(i - 1, 9); v[k][10] = a(i - oy, 10); v[k][11] = a(i - 1 - oy, 11);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (!ok[k]) continue;
+    const int i = c0 + 32 * k;
+    F[cell_at<9>(i, CPIC_F_JFX)] = (R)(cx * (v[k][0] + v[k][1] + v[k][2] + v[k][3]));
+    F[cell_at<9>(i, CPIC_F_JFY)] = (R)(cy * (v[k][4] + v[k][5] + v[k][6] + v[k][7]));
+    F[cell_at<9>(i, CPIC_F_JFZ)] = (R)(cz * (v[k][8] + v[k][9] + v[k][10] + v[k][11]));
+  }
 }
 
 // ------------------------------------------------------------ ghosts
@@ -165,32 +208,69 @@ static int ghost_copy(R* F, const GridDev& g, int m0, cudaStream_t s) {
 // EM_Field_Solver::advance_b (fields.h:692-717): interior cells.
 template <class R>
 __global__ void __launch_bounds__(kThreads)
-advance_b_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz) {
-  int x, y, z;
-  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx, g.ny, g.nz, x, y, z)) return;
-  const int f0 = g.vox(x, y, z), fx = f0 + 1, fy = f0 + g.sx, fz = f0 + g.sx * g.sy;
-  auto e = [&](int c, int m) { return F[cell_at<9>(c, m)]; };
-  const R ex0 = e(f0, CPIC_F_EX), ey0 = e(f0, CPIC_F_EY), ez0 = e(f0, CPIC_F_EZ);
-  F[cell_at<9>(f0, CPIC_F_CBX)] -= (py * (e(fy, CPIC_F_EZ) - ez0) - pz * (e(fz, CPIC_F_EY) - ey0));
-  F[cell_at<9>(f0, CPIC_F_CBY)] -= (pz * (e(fz, CPIC_F_EX) - ex0) - px * (e(fx, CPIC_F_EZ) - ez0));
-  F[cell_at<9>(f0, CPIC_F_CBZ)] -= (px * (e(fx, CPIC_F_EY) - ey0) - py * (e(fy, CPIC_F_EX) - ex0));
+advance_b_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz, int begin, int end) {
+  constexpr int K = 2;
+  const int c0 = lane_cell0<K>(begin);
+  const int oy = g.sx, oz = g.sx * g.sy;
+  auto e = [&](int c, int m) { return __ldg(F + cell_at<9>(c, m)); };  // E is not written here
+  R ex0[K], ey0[K], ez0[K], ezy[K], eyz[K], exz[K], ezx[K], eyx[K], exy[K], bx[K], by[K], bz[K];
+  bool ok[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int f0 = c0 + 32 * k;
+    ok[k] = cell_in_box(f0, end, g, g.nx, g.ny, g.nz);
+    if (ok[k]) {
+      ex0[k] = e(f0, CPIC_F_EX); ey0[k] = e(f0, CPIC_F_EY); ez0[k] = e(f0, CPIC_F_EZ);
+      ezy[k] = e(f0 + oy, CPIC_F_EZ); eyz[k] = e(f0 + oz, CPIC_F_EY);
+      exz[k] = e(f0 + oz, CPIC_F_EX); ezx[k] = e(f0 + 1, CPIC_F_EZ);
+      eyx[k] = e(f0 + 1, CPIC_F_EY); exy[k] = e(f0 + oy, CPIC_F_EX);
+      bx[k] = F[cell_at<9>(f0, CPIC_F_CBX)]; by[k] = F[cell_at<9>(f0, CPIC_F_CBY)];
+      bz[k] = F[cell_at<9>(f0, CPIC_F_CBZ)];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (!ok[k]) continue;
+    const int f0 = c0 + 32 * k;
+    F[cell_at<9>(f0, CPIC_F_CBX)] = bx[k] - (py * (ezy[k] - ez0[k]) - pz * (eyz[k] - ey0[k]));
+    F[cell_at<9>(f0, CPIC_F_CBY)] = by[k] - (pz * (exz[k] - ex0[k]) - px * (ezx[k] - ez0[k]));
+    F[cell_at<9>(f0, CPIC_F_CBZ)] = bz[k] - (px * (eyx[k] - ey0[k]) - py * (exy[k] - ex0[k]));
+  }
 }
 
 // EM_Field_Solver::advance_e (fields.h:646-664): cells [1, n+1] per axis.
 template <class R>
 __global__ void __launch_bounds__(kThreads)
-advance_e_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz, R cj) {
-  int x, y, z;
-  if (!box_coords(blockIdx.x * blockDim.x + threadIdx.x, g.nx + 1, g.ny + 1, g.nz + 1, x, y, z)) return;
-  const int f0 = g.vox(x, y, z), fx = f0 - 1, fy = f0 - g.sx, fz = f0 - g.sx * g.sy;
-  auto b = [&](int c, int m) { return F[cell_at<9>(c, m)]; };
-  const R bx0 = b(f0, CPIC_F_CBX), by0 = b(f0, CPIC_F_CBY), bz0 = b(f0, CPIC_F_CBZ);
-  R* pex = F + cell_at<9>(f0, CPIC_F_EX);
-  R* pey = F + cell_at<9>(f0, CPIC_F_EY);
-  R* pez = F + cell_at<9>(f0, CPIC_F_EZ);
-  *pex = *pex + (-cj * b(f0, CPIC_F_JFX)) + (py * (bz0 - b(fy, CPIC_F_CBZ)) - pz * (by0 - b(fz, CPIC_F_CBY)));
-  *pey = *pey + (-cj * b(f0, CPIC_F_JFY)) + (pz * (bx0 - b(fz, CPIC_F_CBX)) - px * (bz0 - b(fx, CPIC_F_CBZ)));
-  *pez = *pez + (-cj * b(f0, CPIC_F_JFZ)) + (px * (by0 - b(fx, CPIC_F_CBY)) - py * (bx0 - b(fy, CPIC_F_CBX)));
+advance_e_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz, R cj, int begin, int end) {
+  constexpr int K = 2;
+  const int c0 = lane_cell0<K>(begin);
+  const int oy = g.sx, oz = g.sx * g.sy;
+  auto b = [&](int c, int m) { return __ldg(F + cell_at<9>(c, m)); };  // B and J are not written here
+  R bx0[K], by0[K], bz0[K], bzy[K], byz[K], bxz[K], bzx[K], byx[K], bxy[K], jx[K], jy[K], jz[K];
+  R ex[K], ey[K], ez[K];
+  bool ok[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int f0 = c0 + 32 * k;
+    ok[k] = cell_in_box(f0, end, g, g.nx + 1, g.ny + 1, g.nz + 1);
+    if (ok[k]) {
+      bx0[k] = b(f0, CPIC_F_CBX); by0[k] = b(f0, CPIC_F_CBY); bz0[k] = b(f0, CPIC_F_CBZ);
+      bzy[k] = b(f0 - oy, CPIC_F_CBZ); byz[k] = b(f0 - oz, CPIC_F_CBY);
+      bxz[k] = b(f0 - oz, CPIC_F_CBX); bzx[k] = b(f0 - 1, CPIC_F_CBZ);
+      byx[k] = b(f0 - 1, CPIC_F_CBY); bxy[k] = b(f0 - oy, CPIC_F_CBX);
+      jx[k] = b(f0, CPIC_F_JFX); jy[k] = b(f0, CPIC_F_JFY); jz[k] = b(f0, CPIC_F_JFZ);
+      ex[k] = F[cell_at<9>(f0, CPIC_F_EX)]; ey[k] = F[cell_at<9>(f0, CPIC_F_EY)];
+      ez[k] = F[cell_at<9>(f0, CPIC_F_EZ)];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (!ok[k]) continue;
+    const int f0 = c0 + 32 * k;
+    F[cell_at<9>(f0, CPIC_F_EX)] = ex[k] + (-cj * jx[k]) + (py * (bz0[k] - bzy[k]) - pz * (by0[k] - byz[k]));
+    F[cell_at<9>(f0, CPIC_F_EY)] = ey[k] + (-cj * jy[k]) + (pz * (bx0[k] - bxz[k]) - px * (bz0[k] - bzx[k]));
+    F[cell_at<9>(f0, CPIC_F_EZ)] = ez[k] + (-cj * jz[k]) + (px * (by0[k] - byx[k]) - py * (bx0[k] - bxy[k]));
+  }
 }
 
 // ------------------------------------------------------------ energies
@@ -247,7 +327,25 @@ energy_kernel(const R* __restrict__ F, const GridDev g, double* __restrict__ out
   for (unsigned r = warp; r < rows; r += nwarps) {
     const int y = (int)(r % (unsigned)g.ny) + 1, z = (int)(r / (unsigned)g.ny) + 1;
     const int row = g.vox(0, y, z);
-    for (int x = 1 + lane; x <= g.nx; x += 32) {
+    int x = 1 + lane;
+    // four x steps with their 24 loads in flight together; the sums take the
+    // values in the same order as the one-step loop below
+    for (; x + 96 <= g.nx; x += 128) {
+      R v[4][6];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int i = row + x + 32 * j;
+        v[j][0] = F[cell_at<9>(i, CPIC_F_EX)]; v[j][1] = F[cell_at<9>(i, CPIC_F_EY)];
+        v[j][2] = F[cell_at<9>(i, CPIC_F_EZ)]; v[j][3] = F[cell_at<9>(i, CPIC_F_CBX)];
+        v[j][4] = F[cell_at<9>(i, CPIC_F_CBY)]; v[j][5] = F[cell_at<9>(i, CPIC_F_CBZ)];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        ea.add(v[j][0]); ea.add(v[j][1]); ea.add(v[j][2]);
+        ba.add(v[j][3]); ba.add(v[j][4]); ba.add(v[j][5]);
+      }
+    }
+    for (; x <= g.nx; x += 32) {
       const int i = row + x;
       ea.add(F[cell_at<9>(i, CPIC_F_EX)]); ea.add(F[cell_at<9>(i, CPIC_F_EY)]); ea.add(F[cell_at<9>(i, CPIC_F_EZ)]);
       ba.add(F[cell_at<9>(i, CPIC_F_CBX)]); ba.add(F[cell_at<9>(i, CPIC_F_CBY)]); ba.add(F[cell_at<9>(i, CPIC_F_CBZ)]);
@@ -337,8 +435,9 @@ es_energy_kernel(const R* __restrict__ F, int num_cells, double* __restrict__ ou
 // ------------------------------------------------------------ host side
 template <class R>
 static int typed_load_interp(const void* f, void* i, const GridDev& g, cudaStream_t s) {
-  load_interpolator_kernel<R><<<blocks_for((int64_t)g.nx * g.ny * g.nz), kThreads, 0, s>>>(
-      static_cast<const R*>(f), static_cast<R*>(i), g);
+  const CellRange r = cell_range<1>(g, g.nx, g.ny, g.nz);
+  load_interpolator_kernel<R><<<r.blocks, kThreads, 0, s>>>(static_cast<const R*>(f), static_cast<R*>(i), g,
+                                                            r.begin, r.end);
   return launch_status();
 }
 
@@ -350,16 +449,17 @@ static int typed_unload(void* f, const void* a, const GridDev& g, double dx, dou
   const R cx = (R)(0.25 / (double)(R)(rdy * rdz * rdt));
   const R cy = (R)(0.25 / (double)(R)(rdz * rdx * rdt));
   const R cz = (R)(0.25 / (double)(R)(rdx * rdy * rdt));
-  const int64_t n = (int64_t)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
-  unload_kernel<R, Acc><<<blocks_for(n), kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const Acc*>(a),
-                                                           g, (Acc)cx, (Acc)cy, (Acc)cz);
+  const CellRange r = cell_range<2>(g, g.nx + 1, g.ny + 1, g.nz + 1);
+  unload_kernel<R, Acc><<<r.blocks, kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const Acc*>(a), g,
+                                                      (Acc)cx, (Acc)cy, (Acc)cz, r.begin, r.end);
   return launch_status();
 }
 
 template <class R>
 static int typed_advance_b(void* f, double px, double py, double pz, const GridDev& g, cudaStream_t s) {
-  advance_b_kernel<R><<<blocks_for((int64_t)g.nx * g.ny * g.nz), kThreads, 0, s>>>(
-      static_cast<R*>(f), g, (R)px, (R)py, (R)pz);
+  const CellRange r = cell_range<2>(g, g.nx, g.ny, g.nz);
+  advance_b_kernel<R><<<r.blocks, kThreads, 0, s>>>(static_cast<R*>(f), g, (R)px, (R)py, (R)pz, r.begin,
+                                                    r.end);
   int rc = launch_status();
   if (rc) return rc;
   return ghost_copy<R>(static_cast<R*>(f), g, CPIC_F_CBX, s);
@@ -376,8 +476,8 @@ static int typed_advance_e(void* f, double px, double py, double pz, double dt_e
   if (rc) return rc;
   rc = ghost_copy<R>(F, g, CPIC_F_JFX, s);
   if (rc) return rc;
-  const int64_t n = (int64_t)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
-  advance_e_kernel<R><<<blocks_for(n), kThreads, 0, s>>>(F, g, (R)px, (R)py, (R)pz, (R)dt_eps0);
+  const CellRange r = cell_range<2>(g, g.nx + 1, g.ny + 1, g.nz + 1);
+  advance_e_kernel<R><<<r.blocks, kThreads, 0, s>>>(F, g, (R)px, (R)py, (R)pz, (R)dt_eps0, r.begin, r.end);
   return launch_status();
 }
 
