@@ -3,8 +3,7 @@
 Workload (the reference's throughput configuration): uniform thermal plasma,
 128^3 periodic cells, 64 electrons per cell (134,217,728 particles), FP32,
 u_th = 0.05, dt = 0.7 Courant, zero initial fields, particles re-sorted by
-cell every 14 steps (the measured optimum of sort cost against the push's
-growing cost as particles drift out of cell order).  A "step" is the reference's whole time step
+cell every 20 steps.  A "step" is the reference's whole time step
 (example/example.cpp:221-271): interpolator load, accumulator clear, push with
 deposit, accumulator unload, B half step, E step, B half step, field energies,
 plus the amortised sort.  The particle list (4.3 GB) is larger than L2, so no
@@ -36,7 +35,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SORT_INTERVAL = 14
+SORT_INTERVAL = 20
 N_CELLS = 128
 PPC = 64
 TILES = True
