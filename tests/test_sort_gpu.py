@@ -111,3 +111,39 @@ def test_pinned_upload_download_in_pieces():
     torch.cuda.current_stream().synchronize()
     assert np.array_equal(out.numpy(), P.download_bytes())
     assert np.all(np.diff(P.download()["cell"]) >= 0)
+
+
+@pytest.mark.parametrize("kind", ["sorted", "drifted", "random", "out_of_range"])
+@pytest.mark.parametrize("real,vl", [(np.float32, 32), (np.float64, 16)])
+def test_sort_key_patterns(kind, real, vl):
+    """Cell keys as the sort meets them: in cell order (every warp chunk is one
+    or two runs of equal keys), a sorted list after some steps of drift (runs
+    split by strays), random, and with cells outside [0, num_cells) (sorted
+    after every valid cell, in any order among themselves).  The particle
+    records are preserved, and the in-place and out-of-place sorts produce
+    the same key order."""
+    from cabanapic_gb300 import layout as L, pic
+    n = 20011
+    st = random_state(nx=9, ny=7, nz=5, n=n, seed=11, real=real, vl=vl, sort=kind != "random",
+                      disorder=0.2 if kind == "drifted" else 0.0)
+    nc = st["num_cells"]
+    host = dict(st["host"])
+    if kind == "out_of_range":
+        rng = np.random.default_rng(3)
+        bad = rng.random(n) < 0.05
+        host["cell"] = np.where(bad, rng.choice([-7, -1, nc, nc + 3], n), host["cell"]).astype(np.int32)
+    packed = L.pack_particles(host, real, vl)
+    A = pic.ParticleList(n, real, vl).upload(packed)
+    B = pic.ParticleList(n, real, vl).upload(packed)
+    pic.Sorter(A, nc)(A)
+    pic.Sorter(B, nc, double_buffer=True)(B)
+    a, b = A.download(), B.download()
+    key = lambda c: np.where((c >= 0) & (c < nc), c, nc)
+    assert np.all(np.diff(key(a["cell"])) >= 0)
+    assert np.array_equal(key(a["cell"]), key(b["cell"]))
+    ia, ka = _records(a)
+    ib, kb = _records(b)
+    _, k0 = _records(host)
+    i0 = np.lexsort(k0[::-1])
+    for x, y, z in zip(ka, kb, k0):
+        assert np.array_equal(x[ia], y[ib]) and np.array_equal(x[ia], z[i0])
