@@ -173,10 +173,12 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     fields = None
     if WORKLOAD == "diocotron":
         host_packed, fields = decks.diocotron_state(deck, packed=True)
-    elif host_packed is None:
-        host_packed = decks.thermal_particles(deck, packed=True)
+    # host_packed None: the thermal plasma is generated on the device (seeded
+    # Philox, csrc/init.cu) and its initial state copied out for the other legs
     sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup,
                      exact=exact, tiles=TILES, fields=fields)
+    if host_packed is None:
+        host_packed = sim.particles.download_bytes()
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
         sim.step()
@@ -421,7 +423,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload, "particles": n, "cells": deck.num_cells,
                        "l2": f"particle list {n * 32 / 1e9:.2f} GB > 129 MB L2: no flush needed",
-                       "replicas": ws, "push_kernel": "tiled" if TILES else "streaming"},
+                       "replicas": ws, "push_kernel": "tiled" if TILES else "streaming",
+                       "seed": int(deck.extra.get("seed", 2024)),
+                       "rng": "Philox4x32-10 keyed by particle index, generated on the device"},
             "push_ms": push_ms,
             "push_ms_by_step": [round(t, 4) for t in res["push_ms"]],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -34,7 +34,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O2", "-I", INCLUDE, "-I", CSRC]
 CU_UNITS = ["push.cu", "push_fast.cu", "fields.cu", "sort.cu", "diagnostics.cu", "adjoint_fields.cu",
-            "adjoint_push.cu", "uncenter.cu", "dumps.cu"]
+            "adjoint_push.cu", "uncenter.cu", "dumps.cu", "init.cu"]
 # units built with fused multiply-adds (the production push variant)
 FMA_UNITS = {"push_fast.cu"}
 

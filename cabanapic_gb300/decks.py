@@ -208,38 +208,98 @@ def two_stream_1d_particles(deck: Deck) -> dict:
     return {k: v[order] for k, v in out.items()}
 
 
+_PHILOX_M = (np.uint64(0xD2511F53), np.uint64(0xCD9E8D57))
+_PHILOX_W = (0x9E3779B9, 0xBB67AE85)
+_U32 = np.uint64(0xFFFFFFFF)
+
+
+def philox4x32_10(c0, c1, c2, c3, k0: int, k1: int):
+    """Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) over arrays of
+    counters: per round two 32x32->64 products of counter words 0 and 2,
+    their high halves mixed with words 1 and 3 and the key, the key bumped by
+    the Weyl constants.  Returns the four output words (uint32 arrays).  The
+    same generator as the device loader (csrc/init.cu)."""
+    shape = np.broadcast(c0, c1, c2, c3).shape
+    c0, c1, c2, c3 = (np.broadcast_to(np.asarray(c, np.uint64), shape).astype(np.uint64) for c in (c0, c1, c2, c3))
+    k0, k1 = int(k0) & 0xFFFFFFFF, int(k1) & 0xFFFFFFFF
+    for _ in range(10):
+        p0 = c0 * _PHILOX_M[0]
+        p1 = c2 * _PHILOX_M[1]
+        c0, c1, c2, c3 = ((p1 >> np.uint64(32)) ^ c1 ^ np.uint64(k0), p1 & _U32,
+                          (p0 >> np.uint64(32)) ^ c3 ^ np.uint64(k1), p0 & _U32)
+        k0 = (k0 + _PHILOX_W[0]) & 0xFFFFFFFF
+        k1 = (k1 + _PHILOX_W[1]) & 0xFFFFFFFF
+    return tuple(c.astype(np.uint32) for c in (c0, c1, c2, c3))
+
+
+def _thermal_values(p: np.ndarray, R, uth: float, seed: int):
+    """x, y, z, ux, uy, uz of particles p (uint64 indices): counters (p, 0) and
+    (p, 1) under key `seed`; offsets 2u - 1 from 24 (FP32) or 32 (FP64) bits,
+    Box-Muller normals in double rounded once to real_t."""
+    lo, hi = p & _U32, p >> np.uint64(32)
+    k0, k1 = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
+    a = philox4x32_10(lo, hi, 0, 0, k0, k1)
+    b = philox4x32_10(lo, hi, 1, 0, k0, k1)
+    if np.dtype(R) == np.float32:
+        off = [(a[i] >> np.uint32(8)).astype(np.float32) * np.float32(2.0 ** -23) - np.float32(1) for i in range(3)]
+    else:
+        off = [a[i].astype(np.float64) * 2.0 ** -31 - 1.0 for i in range(3)]
+    r1 = np.sqrt(-2.0 * np.log((a[3].astype(np.float64) + 1.0) * 2.0 ** -32))
+    r2 = np.sqrt(-2.0 * np.log((b[1].astype(np.float64) + 1.0) * 2.0 ** -32))
+    t1 = np.pi * (2.0 * (b[0].astype(np.float64) * 2.0 ** -32))
+    t2 = np.pi * (2.0 * (b[2].astype(np.float64) * 2.0 ** -32))
+    mom = [(uth * (r1 * np.cos(t1))).astype(R), (uth * (r1 * np.sin(t1))).astype(R),
+           (uth * (r2 * np.cos(t2))).astype(R)]
+    return off + mom
+
+
 def thermal_particles(deck: Deck, packed: bool = False, n_sample: int = None):
     """Seeded uniform Maxwellian plasma in cell order (ppc particles per
-    interior cell, cells in VOXEL order).  With packed=True returns the AoSoA
-    bytes directly (avoids a second copy at large sizes).  n_sample limits the
-    number of particles generated (every cell keeps its ppc slot pattern: the
-    first n_sample particles)."""
+    interior cell, cells in VOXEL order), on the host: the numpy restatement
+    of the device loader (thermal_particles_device, csrc/init.cu), particle p
+    drawing from Philox4x32-10 counters (p, 0) and (p, 1) under the deck's
+    seed.  Offsets and cells are bit-identical to the device's; momenta agree
+    to the rounding of the libm and CUDA log/cos.  With packed=True returns the
+    AoSoA bytes.  n_sample limits the number of particles generated (the
+    first n_sample of the deck's sequence)."""
     R = deck.R
     p = deck.derived()
     n = deck.num_particles if n_sample is None else int(n_sample)
-    rng = np.random.default_rng(deck.extra.get("seed", 2024))
-    uth = deck.extra.get("uth", 0.05)
+    seed = int(deck.extra.get("seed", 2024))
+    uth = float(deck.extra.get("uth", 0.05))
     nx, ny = deck.nx, deck.ny
-    k = np.arange(n, dtype=np.int64) // deck.nppc
-    ix = k % nx
-    iy = (k // nx) % ny
-    iz = k // (nx * ny)
-    cell = L.voxel(ix + 1, iy + 1, iz + 1, nx, ny).astype(np.int32)
-    del k, ix, iy, iz
-    dt = np.float32 if R is np.float32 else np.float64
-    out = dict(
-        x=(rng.random(n, dtype=dt) * 2 - 1).astype(R, copy=False),
-        y=(rng.random(n, dtype=dt) * 2 - 1).astype(R, copy=False),
-        z=(rng.random(n, dtype=dt) * 2 - 1).astype(R, copy=False),
-        ux=(rng.standard_normal(n, dtype=dt) * uth).astype(R, copy=False),
-        uy=(rng.standard_normal(n, dtype=dt) * uth).astype(R, copy=False),
-        uz=(rng.standard_normal(n, dtype=dt) * uth).astype(R, copy=False),
-        w=np.full(n, p["we"], R),
-        cell=cell,
-    )
+    out = {k: np.empty(n, R) for k in L.PARTICLE_REAL_MEMBERS}
+    out["cell"] = np.empty(n, np.int32)
+    out["w"][:] = p["we"]
+    chunk = 1 << 22
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        idx = np.arange(a, b, dtype=np.uint64)
+        k = (idx // np.uint64(deck.nppc)).astype(np.int64)
+        out["cell"][a:b] = L.voxel(k % nx + 1, (k // nx) % ny + 1, k // (nx * ny) + 1, nx, ny)
+        for key, v in zip(("x", "y", "z", "ux", "uy", "uz"), _thermal_values(idx, R, uth, seed)):
+            out[key][a:b] = v
     if packed:
         return L.pack_particles(out, R, deck.vl)
     return out
+
+
+def is_thermal(deck: Deck) -> bool:
+    return deck.name.startswith("thermal-")
+
+
+def thermal_particles_device(deck: Deck, particles=None, device=None, *, stream=None):
+    """The thermal plasma generated on the device (cpic_thermal_particles):
+    the same particles as thermal_particles, without the host round trip.
+    Fills `particles` (a ParticleList of deck.num_particles) or a new one."""
+    from . import pic
+    from .arrays import ParticleList
+    if particles is None:
+        particles = ParticleList(deck.num_particles, deck.R, deck.vl, device)
+    pic.thermal_particles(particles, deck.nppc, deck.nx, deck.ny, deck.nz,
+                          float(deck.extra.get("uth", 0.05)), float(deck.derived()["we"]),
+                          int(deck.extra.get("seed", 2024)), stream=stream)
+    return particles
 
 
 # ---------------------------------------------------------------- diocotron

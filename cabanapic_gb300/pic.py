@@ -99,6 +99,17 @@ def push(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy
              _STATUS.get().data_ptr(), _stream(stream))
 
 
+def thermal_particles(particles: ParticleList, ppc: int, nx, ny, nz, uth: float, weight: float,
+                      seed: int, *, stream=None) -> None:
+    """Seeded thermal plasma written on the device (cpic_thermal_particles):
+    ppc particles per interior cell in VOXEL order, offsets uniform in
+    [-1, 1), Maxwellian momenta of width uth, weight `weight`; particle p
+    draws from Philox4x32-10 counters (p, 0), (p, 1) under key `seed`."""
+    capi.load().call("cpic_thermal_particles", particles.ptr, particles.n, int(ppc),
+                     C.byref(_grid(nx, ny, nz, 1)), float(uth), float(weight), int(seed) & (2 ** 64 - 1),
+                     particles.precision, particles.vl, _stream(stream))
+
+
 def grid_cells(nx, ny, nz, ng=1) -> int:
     return (nx + 2 * ng) * (ny + 2 * ng) * (nz + 2 * ng)
 

@@ -38,9 +38,12 @@ class Simulation:
         self.fields = FieldArray(nc, R, dev)
         self.solver = pic.EMFieldSolver(self.fields, deck.boundary)
         pic.initialize_interpolator(self.interpolators)
-        if particles is None:
-            particles = D.initial_particles(deck)
-        self.particles.upload(particles)
+        if particles is None and D.is_thermal(deck):
+            D.thermal_particles_device(deck, self.particles)  # seeded, generated in HBM
+        else:
+            if particles is None:
+                particles = D.initial_particles(deck)
+            self.particles.upload(particles)
         if fields is None:
             fields = D.initial_fields(deck)
         if fields is not None:

@@ -221,6 +221,20 @@ int cpic_particle_dump_values(const void* particles, int64_t num_particles, int3
 int cpic_field_dump_values(const void* fields, const cpic_grid* grid, int32_t precision, double xmin,
                            double dx, void* d_out, cpic_stream_t stream);
 
+/* ---------------------------------------------------------------- particle loading
+ * Seeded uniform thermal plasma written on the device (no counterpart in the
+ * reference, whose decks initialise particles on the host:
+ * src/input/deck.h:79-158, decks/custom_init.cxx).  `ppc` particles per
+ * interior cell, cells in VOXEL order with x fastest (particle p in interior
+ * cell p / ppc); offsets uniform in [-1, 1); momenta Maxwellian with width
+ * `uth` per component; every weight `weight`.  Particle p draws from the
+ * counter-based generator Philox4x32-10 at counters (p, 0) and (p, 1) under
+ * the key `seed`, so the list depends only on (seed, p).  Requires
+ * num_particles <= ppc * nx * ny * nz. */
+int cpic_thermal_particles(void* particles, int64_t num_particles, int32_t ppc, const cpic_grid* grid,
+                           double uth, double weight, uint64_t seed, int32_t precision,
+                           int32_t particle_vl, cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- sort
  * Counting sort of the particle list by cell index, in place.  The reference
  * leaves this step commented out (example/example.cpp:226-228, Cabana::sortByKey);

@@ -154,3 +154,38 @@ def test_diocotron_slab_matches_reference_initializers():
     assert np.all(F[..., 5] == np.sqrt(20.0))
     yc = -0.8 + (np.arange(66) - 0.5) * 0.025
     np.testing.assert_array_equal(F[1, :, 7, 1], np.where(yc < -0.1, 0.1, np.where(yc > 0.1, -0.1, -yc)))
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 against the known-answer vectors published with the
+    generator (Random123: zero counter and key; all-ones; the pi digits)."""
+    kats = [((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+            ((0xffffffff,) * 4, (0xffffffff, 0xffffffff), (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+            ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+             (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1))]
+    for ctr, key, want in kats:
+        got = decks.philox4x32_10(*(np.array([c], np.uint64) for c in ctr), *key)
+        assert tuple(int(g[0]) for g in got) == want
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_thermal_stream_is_keyed_by_particle_index(prec):
+    """The thermal loader's values depend only on (seed, particle index): a
+    prefix sample equals the start of the full list, and the Maxwellian and
+    uniform statistics hold."""
+    d = decks.thermal(n=8, ppc=64, precision=prec, num_steps=1, seed=99)
+    full = decks.thermal_particles(d)
+    part = decks.thermal_particles(d, n_sample=1000)
+    for k in full:
+        assert np.array_equal(full[k][:1000], part[k])
+    n = len(full["x"])
+    for k in ("x", "y", "z"):
+        assert full[k].min() >= -1 and full[k].max() < 1
+        assert abs(full[k].astype(np.float64).mean()) < 4 / np.sqrt(3 * n)
+    for k in ("ux", "uy", "uz"):
+        u = full[k].astype(np.float64)
+        assert abs(u.mean()) < 4 * 0.05 / np.sqrt(n)
+        assert abs(u.std() / 0.05 - 1) < 4 / np.sqrt(2 * n)
+    other = decks.thermal_particles(decks.thermal(n=8, ppc=64, precision=prec, num_steps=1, seed=100),
+                                    n_sample=1000)
+    assert not np.array_equal(other["ux"], part["ux"])
