@@ -81,7 +81,7 @@ class _Tracker:
 def run(cells=128, ppc=32, steps=1000, seed=2024, sample_every=1, sort_interval=20) -> dict:
     deck64 = D.thermal(n=cells, ppc=ppc, precision=8, num_steps=steps, seed=seed)
     deck32 = D.thermal(n=cells, ppc=ppc, precision=4, num_steps=steps, seed=seed)
-    host64 = D.thermal_particles(deck64)
+    host64 = D.thermal_particles_device(deck64, device="cuda").download()  # seeded, generated in HBM
     host32 = {k: (v.astype(np.float32) if k != "cell" else v) for k, v in host64.items()}
     host32["w"] = np.full(len(host32["w"]), deck32.derived()["we"], np.float32)
     sims = {"fp32": Simulation(deck32, host32, sort_interval=sort_interval, max_steps=steps),
