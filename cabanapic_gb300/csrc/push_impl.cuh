@@ -52,6 +52,9 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "common.cuh"
 
 #ifndef CPIC_PUSH_NS
@@ -770,16 +773,16 @@ template <class R, int VL, bool LITERAL, bool FAST, class Acc>
 int launch_push(void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
                 int* status, cudaStream_t s) {
   auto kern = push_kernel<R, VL, LITERAL, FAST, Acc>;
-  static int per_sm[64] = {0};
+  static std::atomic<int> per_sm[64];  // blocks per SM, per device (0: not yet queried)
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CPIC_ECUDA;
-  if (per_sm[dev] == 0) {
-    int b = 0;
+  int b = per_sm[dev].load(std::memory_order_relaxed);
+  if (b == 0) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kPushThreads, 0) != cudaSuccess || b < 1) b = 1;
-    per_sm[dev] = b;
+    per_sm[dev].store(b, std::memory_order_relaxed);
   }
   const int64_t chunks = ((int64_t)n + 31) / 32;
-  int64_t blocks = (int64_t)sm_count() * per_sm[dev];
+  int64_t blocks = (int64_t)sm_count() * b;
   const int64_t need = (chunks + kWarps - 1) / kWarps;
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;
@@ -816,26 +819,34 @@ int launch_push_tiled(void* particles, int n, const void* interp, void* acc, con
   auto kern = push_tiled_kernel<R, VL, LITERAL, FAST, Acc>;
   const TileShape ts = tile_shape(a.g);
   const size_t dyn = tiled_dyn_smem<R>(ts.wxmax);
-  static size_t opted[64] = {0};
-  static size_t occ_dyn[64] = {0};
-  static int occ_blocks[64] = {0};
+  // Per device: the largest dynamic shared memory opted in so far (the
+  // attribute only ever grows, under the mutex, so a concurrent launch that
+  // needs less never lowers it under another), and the occupancy for the
+  // last size queried, packed as dyn << 16 | blocks per SM.
+  static std::atomic<size_t> opted[64];
+  static std::atomic<uint64_t> occ[64];
+  static std::mutex opt_in;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CPIC_ECUDA;
   // the 48 KB default covers static + dynamic shared memory: opt in for any size
-  if (opted[dev] < dyn) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
-      return CPIC_ECUDA;
-    opted[dev] = dyn;
+  if (opted[dev].load(std::memory_order_acquire) < dyn) {
+    std::lock_guard<std::mutex> lock(opt_in);
+    if (opted[dev].load(std::memory_order_relaxed) < dyn) {
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
+        return CPIC_ECUDA;
+      opted[dev].store(dyn, std::memory_order_release);
+    }
   }
-  if (occ_dyn[dev] != dyn) {
+  uint64_t o = occ[dev].load(std::memory_order_relaxed);
+  if ((o >> 16) != (uint64_t)dyn) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kTiledThreads, dyn) != cudaSuccess || b < 1) b = 1;
-    occ_blocks[dev] = b;
-    occ_dyn[dev] = dyn;
+    o = ((uint64_t)dyn << 16) | (uint64_t)(b & 0xffff);
+    occ[dev].store(o, std::memory_order_relaxed);
   }
   const int64_t T = 32LL * kConsumers * ts.chunks_per_warp;
   const int64_t ntiles = ((int64_t)n + T - 1) / T;
-  int64_t blocks = (int64_t)sm_count() * occ_blocks[dev];
+  int64_t blocks = (int64_t)sm_count() * (int64_t)(o & 0xffff);
   if (blocks > ntiles) blocks = ntiles;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, kTiledThreads, dyn, s>>>(static_cast<unsigned char*>(particles), n,
