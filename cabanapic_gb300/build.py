@@ -36,7 +36,11 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-
 CU_UNITS = ["push.cu", "push_fast.cu", "fields.cu", "sort.cu", "diagnostics.cu", "adjoint_fields.cu",
             "adjoint_push.cu", "uncenter.cu", "dumps.cu", "init.cu"]
 # units built with fused multiply-adds (the production push variant)
-FMA_UNITS = {"push_fast.cu"}
+FMA_UNITS = {"push_fast.cu", "adjoint_push.cu"}
+# units whose FP32 division and square root may be the fast approximations
+# (the adjoint push: its results are checked against finite differences to a
+# tolerance, not bit for bit)
+FAST_DIV_UNITS = {"adjoint_push.cu"}
 
 
 def _nvcc() -> str:
@@ -75,6 +79,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         flags = list(NVCC_FLAGS)
         if os.path.basename(src) in FMA_UNITS:
             flags[flags.index("--fmad=false")] = "--fmad=true"
+        if os.path.basename(src) in FAST_DIV_UNITS:
+            flags += ["--prec-div=false", "--prec-sqrt=false"]
         log = _run([nvcc, *ARCH, *flags, *extra, "-c", src, "-o", obj])
         return obj, log
 

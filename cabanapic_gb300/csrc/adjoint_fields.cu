@@ -33,15 +33,11 @@ struct Periodic {
   __device__ int zm(int z) const { return z == 1 ? g.nz : z - 1; }
 };
 
-__device__ __forceinline__ bool interior_coords(unsigned t, const GridDev& g, int& x, int& y, int& z) {
-  const unsigned ex = g.nx, ey = g.ny, ez = g.nz;
-  if (t >= ex * ey * ez) return false;
-  const unsigned r = t / ex;
-  x = (int)(t - r * ex) + 1;
-  z = (int)(r / ey);
-  y = (int)(r - (unsigned)z * ey) + 1;
-  z += 1;
-  return true;
+// This thread's interior cell (aligned 32-cell blocks of the linear index).
+__device__ __forceinline__ bool interior_cell(int begin, int end, const GridDev& g, int& j, int& x, int& y,
+                                              int& z) {
+  j = lane_cell0<1, kAdjThreads>(begin);
+  return cell_in_box(j, end, g, g.nx, g.ny, g.nz, x, y, z);
 }
 
 template <class R>
@@ -51,11 +47,10 @@ __device__ __forceinline__ R& fm(R* F, int c, int m) { return F[cell_at<9>(c, m)
 // (src/fields.h:707-709) and coefficients (px, py, pz).
 template <class R>
 __global__ void __launch_bounds__(kAdjThreads)
-adj_advance_b_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz) {
-  int x, y, z;
-  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+adj_advance_b_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz, int begin, int end) {
+  int j, x, y, z;
+  if (!interior_cell(begin, end, g, j, x, y, z)) return;
   const Periodic P{g};
-  const int j = g.vox(x, y, z);
   const int jxm = g.vox(P.xm(x), y, z), jym = g.vox(x, P.ym(y), z), jzm = g.vox(x, y, P.zm(z));
   const R bx = fm(L, j, CPIC_F_CBX), by = fm(L, j, CPIC_F_CBY), bz = fm(L, j, CPIC_F_CBZ);
   const R tex = pz * (fm(L, jzm, CPIC_F_CBY) - by) - py * (fm(L, jym, CPIC_F_CBZ) - bz);
@@ -70,11 +65,10 @@ adj_advance_b_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz) {
 // backward-difference curl of advance_e (src/fields.h:655-657).
 template <class R>
 __global__ void __launch_bounds__(kAdjThreads)
-adj_advance_e_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz, R cj) {
-  int x, y, z;
-  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+adj_advance_e_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz, R cj, int begin, int end) {
+  int j, x, y, z;
+  if (!interior_cell(begin, end, g, j, x, y, z)) return;
   const Periodic P{g};
-  const int j = g.vox(x, y, z);
   const int jxp = g.vox(P.xp(x), y, z), jyp = g.vox(x, P.yp(y), z), jzp = g.vox(x, y, P.zp(z));
   const R ex = fm(L, j, CPIC_F_EX), ey = fm(L, j, CPIC_F_EY), ez = fm(L, j, CPIC_F_EZ);
   fm(L, j, CPIC_F_CBX) += pz * (ey - fm(L, jzp, CPIC_F_EY)) - py * (ez - fm(L, jyp, CPIC_F_EZ));
@@ -89,11 +83,10 @@ adj_advance_e_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz, R cj)
 // with the jf fold); writes the 12 adjoint accumulators of every interior cell.
 template <class R>
 __global__ void __launch_bounds__(kAdjThreads)
-adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R cx, R cy, R cz) {
-  int x, y, z;
-  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R cx, R cy, R cz, int begin, int end) {
+  int c, x, y, z;
+  if (!interior_cell(begin, end, g, c, x, y, z)) return;
   const Periodic P{g};
-  const int c = g.vox(x, y, z);
   const int xp = P.xp(x), yp = P.yp(y), zp = P.zp(z);
   auto lj = [&](int cc, int m) { return L[cell_at<9>(cc, m)]; };
   R* a = A + (size_t)c * 12;
@@ -116,11 +109,10 @@ adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R
 // to four cells (E) or two cells (B); gathered per field cell.
 template <class R>
 __global__ void __launch_bounds__(kAdjThreads)
-adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g) {
-  int x, y, z;
-  if (!interior_coords(blockIdx.x * blockDim.x + threadIdx.x, g, x, y, z)) return;
+adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g, int begin, int end) {
+  int j, x, y, z;
+  if (!interior_cell(begin, end, g, j, x, y, z)) return;
   const Periodic P{g};
-  const int j = g.vox(x, y, z);
   const int xm = P.xm(x), ym = P.ym(y), zm = P.zm(z);
   auto li = [&](int c, int m) { return LI[cell_at<18>(c, m)]; };
   const R q = 0.25, h = 0.5;
@@ -148,10 +140,7 @@ adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g) 
                           h * (li(g.vox(x, y, zm), CPIC_I_CBZ) + li(g.vox(x, y, zm), CPIC_I_DCBZDZ));
 }
 
-inline unsigned nblocks(const GridDev& g) {
-  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
-  return (unsigned)((n + kAdjThreads - 1) / kAdjThreads);
-}
+inline CellRange interior_range(const GridDev& g) { return cell_range<1, kAdjThreads>(g, g.nx, g.ny, g.nz); }
 
 }  // namespace
 }  // namespace cpic
@@ -163,6 +152,7 @@ using namespace cpic;
   if (rc) return rc;                                                      \
   if (precision != CPIC_FLOAT && precision != CPIC_DOUBLE) return CPIC_EINVAL; \
   const GridDev g = make_grid(grid);                                      \
+  const CellRange r = interior_range(g);                                  \
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream)
 
 extern "C" int cpic_adjoint_advance_b(void* d_lambda_fields, double px, double py, double pz,
@@ -170,11 +160,11 @@ extern "C" int cpic_adjoint_advance_b(void* d_lambda_fields, double px, double p
   ADJ_PREAMBLE();
   if (!d_lambda_fields) return CPIC_EINVAL;
   if (precision == CPIC_FLOAT)
-    adj_advance_b_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<float*>(d_lambda_fields), g,
-                                                                   (float)px, (float)py, (float)pz);
+    adj_advance_b_kernel<float><<<r.blocks, kAdjThreads, 0, s>>>(static_cast<float*>(d_lambda_fields), g,
+                                                                   (float)px, (float)py, (float)pz, r.begin, r.end);
   else
-    adj_advance_b_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<double*>(d_lambda_fields), g,
-                                                                    px, py, pz);
+    adj_advance_b_kernel<double><<<r.blocks, kAdjThreads, 0, s>>>(static_cast<double*>(d_lambda_fields), g,
+                                                                    px, py, pz, r.begin, r.end);
   return launch_status();
 }
 
@@ -184,12 +174,12 @@ extern "C" int cpic_adjoint_advance_e(void* d_lambda_fields, double px, double p
   ADJ_PREAMBLE();
   if (!d_lambda_fields) return CPIC_EINVAL;
   if (precision == CPIC_FLOAT)
-    adj_advance_e_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<float*>(d_lambda_fields), g,
+    adj_advance_e_kernel<float><<<r.blocks, kAdjThreads, 0, s>>>(static_cast<float*>(d_lambda_fields), g,
                                                                    (float)px, (float)py, (float)pz,
-                                                                   (float)dt_eps0);
+                                                                   (float)dt_eps0, r.begin, r.end);
   else
-    adj_advance_e_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<double*>(d_lambda_fields), g,
-                                                                    px, py, pz, dt_eps0);
+    adj_advance_e_kernel<double><<<r.blocks, kAdjThreads, 0, s>>>(static_cast<double*>(d_lambda_fields), g,
+                                                                    px, py, pz, dt_eps0, r.begin, r.end);
   return launch_status();
 }
 
@@ -200,14 +190,14 @@ extern "C" int cpic_adjoint_unload_accumulator(const void* d_lambda_fields, void
   if (!d_lambda_fields || !d_lambda_acc) return CPIC_EINVAL;
   if (precision == CPIC_FLOAT) {
     const float rdx = (float)dx, rdy = (float)dy, rdz = (float)dz, rdt = (float)dt;
-    adj_unload_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(
+    adj_unload_kernel<float><<<r.blocks, kAdjThreads, 0, s>>>(
         static_cast<const float*>(d_lambda_fields), static_cast<float*>(d_lambda_acc), g,
         (float)(0.25 / (double)(float)(rdy * rdz * rdt)), (float)(0.25 / (double)(float)(rdz * rdx * rdt)),
-        (float)(0.25 / (double)(float)(rdx * rdy * rdt)));
+        (float)(0.25 / (double)(float)(rdx * rdy * rdt)), r.begin, r.end);
   } else {
-    adj_unload_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(
+    adj_unload_kernel<double><<<r.blocks, kAdjThreads, 0, s>>>(
         static_cast<const double*>(d_lambda_fields), static_cast<double*>(d_lambda_acc), g,
-        0.25 / (dy * dz * dt), 0.25 / (dz * dx * dt), 0.25 / (dx * dy * dt));
+        0.25 / (dy * dz * dt), 0.25 / (dz * dx * dt), 0.25 / (dx * dy * dt), r.begin, r.end);
   }
   return launch_status();
 }
@@ -218,10 +208,10 @@ extern "C" int cpic_adjoint_load_interpolator(const void* d_lambda_interp, void*
   ADJ_PREAMBLE();
   if (!d_lambda_interp || !d_lambda_fields) return CPIC_EINVAL;
   if (precision == CPIC_FLOAT)
-    adj_interp_kernel<float><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<const float*>(d_lambda_interp),
-                                                                static_cast<float*>(d_lambda_fields), g);
+    adj_interp_kernel<float><<<r.blocks, kAdjThreads, 0, s>>>(static_cast<const float*>(d_lambda_interp),
+                                                                static_cast<float*>(d_lambda_fields), g, r.begin, r.end);
   else
-    adj_interp_kernel<double><<<nblocks(g), kAdjThreads, 0, s>>>(static_cast<const double*>(d_lambda_interp),
-                                                                 static_cast<double*>(d_lambda_fields), g);
+    adj_interp_kernel<double><<<r.blocks, kAdjThreads, 0, s>>>(static_cast<const double*>(d_lambda_interp),
+                                                                 static_cast<double*>(d_lambda_fields), g, r.begin, r.end);
   return launch_status();
 }

@@ -82,29 +82,71 @@ __device__ __forceinline__ void set_comp(V3<R>& v, int a, R val) {
   if (a == 0) v.x = val; else if (a == 1) v.y = val; else v.z = val;
 }
 
+// One streak of the forward split (move_p.h:93-371; an in-cell move is one
+// streak with axis 3): from the streak's start (pos, rem, c) returns its
+// half-length `len` and face `axis`, and advances (pos, rem, c) to the next
+// streak's start.
+template <class R>
+__device__ __forceinline__ void streak_step(V3<R>& pos, V3<R>& rem, int& c, bool inb, const GridDev& g,
+                                            R& len, int& axis) {
+  axis = 3;
+  len = 2;
+  if (!inb) {
+    for (int ax = 0; ax < 3; ++ax) {
+      const R r = comp(rem, ax);
+      const R dir = r > 0 ? R(1) : R(-1);
+      const R fr = (r == 0) ? R(3.4e38) : (dir - comp(pos, ax)) / r;
+      if (fr < len) { len = fr; axis = ax; }
+    }
+  }
+  len *= R(0.5);
+  const V3<R> s{rem.x * len, rem.y * len, rem.z * len};
+  // the face direction is the sign of the remaining displacement (move_p.h:109-111)
+  const R dir = axis < 3 && comp(rem, axis) > 0 ? R(1) : R(-1);
+  rem = {rem.x - s.x, rem.y - s.y, rem.z - s.z};
+  pos = {pos.x + s.x + s.x, pos.y + s.y + s.y, pos.z + s.z + s.z};
+  if (axis == 3) return;
+  int ix = c, iy, iz;  // RANK_TO_INDEX (src/types.h:184-193)
+  iy = div_magic(ix, g.dsx); ix -= iy * g.sx;
+  iz = div_magic(iy, g.dsy); iy -= iz * g.sy;
+  const int step = dir > 0 ? 1 : -1;
+  if (axis == 0) ix += step; else if (axis == 1) iy += step; else iz += step;
+  if (ix == 0) ix = g.nx; else if (ix == g.nx + 1) ix = 1;
+  if (iy == 0) iy = g.ny; else if (iy == g.ny + 1) iy = 1;
+  if (iz == 0) iz = g.nz; else if (iz == g.nz + 1) iz = 1;
+  c = g.vox(ix, iy, iz);
+  set_comp(pos, axis, -dir);
+}
+
+// The adjoint of one particle's push.  Writes lambda_x, lambda_u in place and
+// returns the 18 interpolator adjoints of its cell in lf; false (nothing
+// written, lf unset) for a particle the kernel cannot take.
 template <class R, int VL, bool LITERAL>
-__global__ void __launch_bounds__(kAdjThreads)
-adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
-                    const R* __restrict__ lacc, unsigned char* __restrict__ lpart, R* __restrict__ linterp,
-                    const AdjArgs<R> a, int* __restrict__ status) {
+__device__ __forceinline__ bool adjoint_one(const unsigned char* __restrict__ part, int64_t p,
+                                            const R* __restrict__ interp, const R* __restrict__ lacc,
+                                            unsigned char* __restrict__ lpart, const AdjArgs<R>& a,
+                                            int* __restrict__ status, int& cell, R lf[18]) {
   using L = PLayout<R, VL>;
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
   auto mem = [&](const unsigned char* b, int m) { return *reinterpret_cast<const R*>(b + L::off(p, m)); };
   const V3<R> x0{mem(part, 0), mem(part, 1), mem(part, 2)};
   const V3<R> u0{mem(part, 3), mem(part, 4), mem(part, 5)};
   const R w = mem(part, 6);
-  const int cell = *reinterpret_cast<const int*>(part + L::cell_off(p));
+  cell = *reinterpret_cast<const int*>(part + L::cell_off(p));
   const V3<R> lxo{mem(lpart, 0), mem(lpart, 1), mem(lpart, 2)};
   const V3<R> luo{mem(lpart, 3), mem(lpart, 4), mem(lpart, 5)};
   if ((unsigned)cell >= (unsigned)a.g.num_cells) {
     atomicOr(status, CPIC_STATUS_CELL_RANGE);
-    return;
+    return false;
   }
   const R one = 1, k = a.qdt_2mc;
   R f[18];
 #pragma unroll
   for (int m = 0; m < 18; ++m) f[m] = __ldg(interp + cell_at<18>(cell, m));
+  // the accumulator adjoint of the particle's own cell, read with the
+  // coefficients (every streak but a crosser's later ones deposits there)
+  R la0[12];
+#pragma unroll
+  for (int m = 0; m < 12; ++m) la0[m] = __ldg(lacc + (size_t)cell * 12 + m);
 
   // ---------------- forward recompute (push.h:124-182)
   const V3<R> ha{k * ((f[0] + x0.y * f[1]) + x0.z * (f[2] + x0.y * f[3])),
@@ -130,61 +172,42 @@ adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __re
   const V3<R> d{cu.x * rg, cu.y * rg, cu.z * rg};
   const R q = w * a.qsp;
 
-  // streak split (move_p.h:93-371; an in-cell move is one streak with axis 3)
-  V3<R> spos[kMaxAdjStreaks], srem[kMaxAdjStreaks];
-  R slen[kMaxAdjStreaks];
-  int saxis[kMaxAdjStreaks], scell[kMaxAdjStreaks];
+
+  // streak split: count the streaks (their states are replayed in reverse)
+  const V3<R> np{x0.x + R(2) * d.x, x0.y + R(2) * d.y, x0.z + R(2) * d.z};
+  const bool inb = np.x <= one && np.y <= one && np.z <= one && -np.x <= one && -np.y <= one &&
+                   -np.z <= one;
   int ns = 0;
   {
     V3<R> pos = x0, rem = d;
     int c = cell;
-    const V3<R> np{x0.x + R(2) * d.x, x0.y + R(2) * d.y, x0.z + R(2) * d.z};
-    const bool inb = np.x <= one && np.y <= one && np.z <= one && -np.x <= one && -np.y <= one &&
-                     -np.z <= one;
     bool done = false;
     for (int it = 0; it < kMaxAdjStreaks; ++it) {
-      int axis = 3;
-      R len = 2;
-      if (!inb) {
-        for (int ax = 0; ax < 3; ++ax) {
-          const R r = comp(rem, ax);
-          const R dir = r > 0 ? R(1) : R(-1);
-          const R fr = (r == 0) ? R(3.4e38) : (dir - comp(pos, ax)) / r;
-          if (fr < len) { len = fr; axis = ax; }
-        }
-      }
-      len *= R(0.5);
-      spos[ns] = pos; srem[ns] = rem; slen[ns] = len; saxis[ns] = axis; scell[ns] = c;
+      R len;
+      int axis;
+      streak_step<R>(pos, rem, c, inb, a.g, len, axis);
       ++ns;
-      const V3<R> s{rem.x * len, rem.y * len, rem.z * len};
-      // the face direction is the sign of the remaining displacement (move_p.h:109-111)
-      const R dir = axis < 3 && comp(rem, axis) > 0 ? R(1) : R(-1);
-      rem = {rem.x - s.x, rem.y - s.y, rem.z - s.z};
-      pos = {pos.x + s.x + s.x, pos.y + s.y + s.y, pos.z + s.z + s.z};
       if (axis == 3) { done = true; break; }
-      int ix = c, iy, iz;
-      iy = ix / a.g.sx; ix -= iy * a.g.sx;
-      iz = iy / a.g.sy; iy -= iz * a.g.sy;
-      const int step = dir > 0 ? 1 : -1;
-      if (axis == 0) ix += step; else if (axis == 1) iy += step; else iz += step;
-      if (ix == 0) ix = a.g.nx; else if (ix == a.g.nx + 1) ix = 1;
-      if (iy == 0) iy = a.g.ny; else if (iy == a.g.ny + 1) iy = 1;
-      if (iz == 0) iz = a.g.nz; else if (iz == a.g.nz + 1) iz = 1;
-      c = a.g.vox(ix, iy, iz);
-      set_comp(pos, axis, -dir);
     }
     if (!done) {
       atomicOr(status, CPIC_STATUS_MOVER_CAP);
-      return;
+      return false;
     }
   }
 
-  // ---------------- reverse: streaks (last to first)
+  // ---------------- reverse: streaks (last to first), each replayed from the start
   V3<R> lpos = lxo, lrem{0, 0, 0};
   for (int kk = ns - 1; kk >= 0; --kk) {
-    const int ax = saxis[kk];
-    const R len = slen[kk];
-    const V3<R> pos = spos[kk], rem = srem[kk];
+    V3<R> pos = x0, rem = d;
+    int c = cell;
+    R len;
+    int ax;
+    for (int j = 0; j < kk; ++j) streak_step<R>(pos, rem, c, inb, a.g, len, ax);
+    {
+      V3<R> pos1 = pos, rem1 = rem;
+      int c1 = c;
+      streak_step<R>(pos1, rem1, c1, inb, a.g, len, ax);
+    }
     const V3<R> s{rem.x * len, rem.y * len, rem.z * len};
     const V3<R> mid{pos.x + s.x, pos.y + s.y, pos.z + s.z};
     V3<R> ls{0, 0, 0}, lm{0, 0, 0}, lp{0, 0, 0};
@@ -199,9 +222,14 @@ adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __re
     ls = {ls.x - lrem.x, ls.y - lrem.y, ls.z - lrem.z};
     // deposit of the streak into its cell
     R la[12];
-    const R* ap = lacc + (size_t)scell[kk] * 12;
+    if (c == cell) {
 #pragma unroll
-    for (int m = 0; m < 12; ++m) la[m] = __ldg(ap + m);
+      for (int m = 0; m < 12; ++m) la[m] = la0[m];
+    } else {
+      const R* ap = lacc + (size_t)c * 12;
+#pragma unroll
+      for (int m = 0; m < 12; ++m) la[m] = __ldg(ap + m);
+    }
     deposit_adjoint<R>(q, s, mid, la, ls, lm);
     // mid = pos + s
     lp = {lp.x + lm.x, lp.y + lm.y, lp.z + lm.z};
@@ -256,7 +284,6 @@ adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __re
   lha = {lha.x + lu1.x, lha.y + lu1.y, lha.z + lu1.z};
 
   // ---------------- reverse: field at the particle (push.h:124-138)
-  R lf[18];
   lf[0] = k * lha.x;
   lf[1] = k * x0.y * lha.x;
   lf[2] = k * x0.z * lha.x;
@@ -283,10 +310,85 @@ adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __re
   auto put = [&](int m, R v) { *reinterpret_cast<R*>(lpart + L::off(p, m)) = v; };
   put(0, lx.x); put(1, lx.y); put(2, lx.z);
   put(3, lu1.x); put(4, lu1.y); put(5, lu1.z);
-  // transpose of the gather
-  R* li = linterp;
+  return true;
+}
+
+// Sum of v[0..17] over the 32 lanes, scattered: afterwards lane l holds the
+// total of value index value18_of_lane(l) (18 lanes hold distinct values).
+// Halving levels over 18 -> 9 -> 5 -> 3 -> 2 -> 1 values (odd counts padded
+// with a zero): 20 shuffles.
+template <class R>
+__device__ __forceinline__ R reduce_scatter18(const R v[18], int lane) {
+  const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4, h2 = lane & 2, h1 = lane & 1;
+  R a9[9];
 #pragma unroll
-  for (int m = 0; m < 18; ++m) red_add(li + cell_at<18>(cell, m), lf[m]);
+  for (int k = 0; k < 9; ++k)
+    a9[k] = (h16 ? v[k + 9] : v[k]) + __shfl_xor_sync(kFull, h16 ? v[k] : v[k + 9], 16);
+  R b5[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const R hi = k + 5 < 9 ? a9[k + 5] : R(0);
+    b5[k] = (h8 ? hi : a9[k]) + __shfl_xor_sync(kFull, h8 ? a9[k] : hi, 8);
+  }
+  R c3[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const R hi = k + 3 < 5 ? b5[k + 3] : R(0);
+    c3[k] = (h4 ? hi : b5[k]) + __shfl_xor_sync(kFull, h4 ? b5[k] : hi, 4);
+  }
+  R d2[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const R hi = k + 2 < 3 ? c3[k + 2] : R(0);
+    d2[k] = (h2 ? hi : c3[k]) + __shfl_xor_sync(kFull, h2 ? c3[k] : hi, 2);
+  }
+  return (h1 ? d2[1] : d2[0]) + __shfl_xor_sync(kFull, h1 ? d2[0] : d2[1], 1);
+}
+
+// Value index held by `lane` after reduce_scatter18, or -1.
+__device__ __forceinline__ int value18_of_lane(int lane) {
+  const int i4 = 2 * ((lane >> 1) & 1) + (lane & 1);
+  if (i4 >= 3) return -1;
+  const int i3 = 3 * ((lane >> 2) & 1) + i4;
+  if (i3 >= 5) return -1;
+  const int i2 = 5 * ((lane >> 3) & 1) + i3;
+  if (i2 >= 9) return -1;
+  return 9 * ((lane >> 4) & 1) + i2;
+}
+
+template <class R, int VL, bool LITERAL>
+__global__ void __launch_bounds__(kAdjThreads)
+adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
+                    const R* __restrict__ lacc, unsigned char* __restrict__ lpart, R* __restrict__ linterp,
+                    const AdjArgs<R> a, int* __restrict__ status) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = (int)(threadIdx.x & 31);
+  R lf[18];
+  int cell = 0;
+  const bool dep = p < n && adjoint_one<R, VL, LITERAL>(part, p, interp, lacc, lpart, a, status, cell, lf);
+  // transpose of the gather: the largest group of lanes sharing a cell is
+  // reduced over the warp (18 atomics for the group), the others add their own
+  const int key = dep ? cell : -1 - lane;
+  const unsigned peers = __match_any_sync(kFull, key);
+  const unsigned score = dep ? ((unsigned)__popc(peers) << 5) | (unsigned)(31 - (__ffs(peers) - 1)) : 0u;
+  const unsigned best = __reduce_max_sync(kFull, score);
+  const int bsize = (int)(best >> 5);
+  const int leader = 31 - (int)(best & 31);
+  bool in_major = false;
+  if (bsize >= 2) {  // warp-uniform
+    in_major = dep && ((peers >> leader) & 1u);
+    R w[18];
+#pragma unroll
+    for (int m = 0; m < 18; ++m) w[m] = in_major ? lf[m] : R(0);
+    const R tot = reduce_scatter18<R>(w, lane);
+    const int major_cell = __shfl_sync(kFull, cell, leader);
+    const int vi = value18_of_lane(lane);
+    if (vi >= 0) red_add(linterp + cell_at<18>(major_cell, vi), tot);
+  }
+  if (dep && !in_major) {
+#pragma unroll
+    for (int m = 0; m < 18; ++m) red_add(linterp + cell_at<18>(cell, m), lf[m]);
+  }
 }
 
 template <class R, int VL, bool LITERAL>

@@ -53,6 +53,49 @@ inline GridDev make_grid(const cpic_grid* g) {
   return d;
 }
 
+// Launch shape of the per-cell stencil kernels: each warp takes K
+// consecutive 32-cell AoSoA blocks of the linear cell index, so a warp's
+// access to one member is one aligned 128-byte line, and a lane skips a cell
+// outside the kernel's box [1, hx] x [1, hy] x [1, hz].
+struct CellRange {
+  int begin, end;   // linear cells [begin, end); begin is a multiple of 32
+  unsigned blocks;  // launch grid of THREADS-thread blocks
+};
+
+template <int K, int THREADS>
+inline CellRange cell_range(const GridDev& g, int hx, int hy, int hz) {
+  CellRange r;
+  r.begin = g.vox(1, 1, 1) & ~31;
+  r.end = g.vox(hx, hy, hz) + 1;
+  const int64_t warps = ((int64_t)(r.end - r.begin) + 32 * K - 1) / (32 * K);
+  const int64_t blocks = (warps * 32 + THREADS - 1) / THREADS;
+  r.blocks = (unsigned)(blocks < 1 ? 1 : blocks);
+  return r;
+}
+
+// This lane's cell in the first of its warp's K blocks (the k-th is 32 k on).
+template <int K, int THREADS>
+__device__ __forceinline__ int lane_cell0(int begin) {
+  const int64_t warp = (int64_t)blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5);
+  return (int)(begin + warp * (32 * K) + (threadIdx.x & 31));
+}
+
+// Whether cell c (< end) lies in the box, with its coordinates.
+__device__ __forceinline__ bool cell_in_box(int c, int end, const GridDev& g, int hx, int hy, int hz,
+                                            int& x, int& y, int& z) {
+  if (c >= end) return false;
+  y = div_magic(c, g.dsx);
+  x = c - y * g.sx;
+  z = div_magic(y, g.dsy);
+  y -= z * g.sy;
+  return x >= 1 && x <= hx && y >= 1 && y <= hy && z >= 1 && z <= hz;
+}
+
+__device__ __forceinline__ bool cell_in_box(int c, int end, const GridDev& g, int hx, int hy, int hz) {
+  int x, y, z;
+  return cell_in_box(c, end, g, hx, hy, hz, x, y, z);
+}
+
 // Member m of cell c in a cell AoSoA with NM members (interpolator 18, field 9).
 template <int NM>
 __host__ __device__ __forceinline__ size_t cell_at(int c, int m) {

@@ -27,48 +27,12 @@ inline unsigned blocks_for(int64_t n, int threads = kThreads) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
-// The stencil kernels map each warp to K consecutive 32-cell AoSoA blocks of
-// the linear cell index, so a warp's access to one member is one aligned
-// 128-byte line, and a lane skips a cell outside the kernel's box
-// [1, hx] x [1, hy] x [1, hz].  Each thread issues the loads of all its cells
-// before storing any result.
-struct CellRange {
-  int begin, end;   // linear cells [begin, end); begin is a multiple of 32
-  unsigned blocks;  // launch grid of kThreads-thread blocks
-};
-
-template <int K>
-inline CellRange cell_range(const GridDev& g, int hx, int hy, int hz) {
-  CellRange r;
-  r.begin = g.vox(1, 1, 1) & ~31;
-  r.end = g.vox(hx, hy, hz) + 1;
-  const int64_t warps = ((int64_t)(r.end - r.begin) + 32 * K - 1) / (32 * K);
-  r.blocks = blocks_for(warps * 32);
-  return r;
-}
-
-// This lane's cell in the first of its warp's K blocks (the k-th is 32 k on).
-template <int K>
-__device__ __forceinline__ int lane_cell0(int begin) {
-  const int64_t warp = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
-  return (int)(begin + warp * (32 * K) + (threadIdx.x & 31));
-}
-
-__device__ __forceinline__ bool cell_in_box(int c, int end, const GridDev& g, int hx, int hy, int hz) {
-  if (c >= end) return false;
-  int y = div_magic(c, g.dsx);
-  const int x = c - y * g.sx;
-  const int z = div_magic(y, g.dsy);
-  y -= z * g.sy;
-  return x >= 1 && x <= hx && y >= 1 && y <= hy && z >= 1 && z <= hz;
-}
-
 // ------------------------------------------------------------ interpolator
 // load_interpolator_array (interpolator.cpp:48-136): interior cells.
 template <class R>
 __global__ void __launch_bounds__(kThreads)
 load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridDev g, int begin, int end) {
-  const int i = lane_cell0<1>(begin);
+  const int i = lane_cell0<1, kThreads>(begin);
   if (!cell_in_box(i, end, g, g.nx, g.ny, g.nz)) return;
   const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
   const R fourth = 1.0 / 4.0, half = 1.0 / 2.0;
@@ -106,7 +70,7 @@ __global__ void __launch_bounds__(kThreads)
 unload_kernel(R* __restrict__ F, const Acc* __restrict__ A, const GridDev g, Acc cx, Acc cy, Acc cz,
               int begin, int end) {
   constexpr int K = 2;
-  const int c0 = lane_cell0<K>(begin);
+  const int c0 = lane_cell0<K, kThreads>(begin);
   const int oy = g.sx, oz = g.sx * g.sy;
   auto a = [&](int c, int k) { return __ldg(A + (size_t)c * 12 + k); };
   Acc v[K][12];
@@ -210,7 +174,7 @@ template <class R>
 __global__ void __launch_bounds__(kThreads)
 advance_b_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz, int begin, int end) {
   constexpr int K = 2;
-  const int c0 = lane_cell0<K>(begin);
+  const int c0 = lane_cell0<K, kThreads>(begin);
   const int oy = g.sx, oz = g.sx * g.sy;
   auto e = [&](int c, int m) { return __ldg(F + cell_at<9>(c, m)); };  // E is not written here
   R ex0[K], ey0[K], ez0[K], ezy[K], eyz[K], exz[K], ezx[K], eyx[K], exy[K], bx[K], by[K], bz[K];
@@ -243,7 +207,7 @@ template <class R>
 __global__ void __launch_bounds__(kThreads)
 advance_e_kernel(R* __restrict__ F, const GridDev g, R px, R py, R pz, R cj, int begin, int end) {
   constexpr int K = 2;
-  const int c0 = lane_cell0<K>(begin);
+  const int c0 = lane_cell0<K, kThreads>(begin);
   const int oy = g.sx, oz = g.sx * g.sy;
   auto b = [&](int c, int m) { return __ldg(F + cell_at<9>(c, m)); };  // B and J are not written here
   R bx0[K], by0[K], bz0[K], bzy[K], byz[K], bxz[K], bzx[K], byx[K], bxy[K], jx[K], jy[K], jz[K];
@@ -435,7 +399,7 @@ es_energy_kernel(const R* __restrict__ F, int num_cells, double* __restrict__ ou
 // ------------------------------------------------------------ host side
 template <class R>
 static int typed_load_interp(const void* f, void* i, const GridDev& g, cudaStream_t s) {
-  const CellRange r = cell_range<1>(g, g.nx, g.ny, g.nz);
+  const CellRange r = cell_range<1, kThreads>(g, g.nx, g.ny, g.nz);
   load_interpolator_kernel<R><<<r.blocks, kThreads, 0, s>>>(static_cast<const R*>(f), static_cast<R*>(i), g,
                                                             r.begin, r.end);
   return launch_status();
@@ -449,7 +413,7 @@ static int typed_unload(void* f, const void* a, const GridDev& g, double dx, dou
   const R cx = (R)(0.25 / (double)(R)(rdy * rdz * rdt));
   const R cy = (R)(0.25 / (double)(R)(rdz * rdx * rdt));
   const R cz = (R)(0.25 / (double)(R)(rdx * rdy * rdt));
-  const CellRange r = cell_range<2>(g, g.nx + 1, g.ny + 1, g.nz + 1);
+  const CellRange r = cell_range<2, kThreads>(g, g.nx + 1, g.ny + 1, g.nz + 1);
   unload_kernel<R, Acc><<<r.blocks, kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const Acc*>(a), g,
                                                       (Acc)cx, (Acc)cy, (Acc)cz, r.begin, r.end);
   return launch_status();
@@ -457,7 +421,7 @@ static int typed_unload(void* f, const void* a, const GridDev& g, double dx, dou
 
 template <class R>
 static int typed_advance_b(void* f, double px, double py, double pz, const GridDev& g, cudaStream_t s) {
-  const CellRange r = cell_range<2>(g, g.nx, g.ny, g.nz);
+  const CellRange r = cell_range<2, kThreads>(g, g.nx, g.ny, g.nz);
   advance_b_kernel<R><<<r.blocks, kThreads, 0, s>>>(static_cast<R*>(f), g, (R)px, (R)py, (R)pz, r.begin,
                                                     r.end);
   int rc = launch_status();
@@ -476,7 +440,7 @@ static int typed_advance_e(void* f, double px, double py, double pz, double dt_e
   if (rc) return rc;
   rc = ghost_copy<R>(F, g, CPIC_F_JFX, s);
   if (rc) return rc;
-  const CellRange r = cell_range<2>(g, g.nx + 1, g.ny + 1, g.nz + 1);
+  const CellRange r = cell_range<2, kThreads>(g, g.nx + 1, g.ny + 1, g.nz + 1);
   advance_e_kernel<R><<<r.blocks, kThreads, 0, s>>>(F, g, (R)px, (R)py, (R)pz, (R)dt_eps0, r.begin, r.end);
   return launch_status();
 }
