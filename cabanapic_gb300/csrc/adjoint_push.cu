@@ -10,12 +10,17 @@
 // is a gather from the adjoint currents) -- the kernel recomputes the forward
 // push from the step's starting state and returns lambda_x, lambda_u (the
 // adjoint before the step, written in place) and adds lambda_f to the
-// adjoint interpolator array (the transpose of the gather, by atomics).
+// adjoint interpolator array (the transpose of the gather: reduced over the
+// warp's largest group of lanes sharing a cell, then atomics).
 //
 // Cell indices are piecewise constant: the streak split (which face is hit
 // first, how many streaks) is taken from the forward recompute, and the
 // derivative flows through the streak lengths and midpoints.  The particle
 // weight is not differentiated.
+//
+// This unit is built with fused multiply-adds and the fast FP32 divide and
+// square root (cabanapic_gb300/build.py): its results are held to finite
+// differences within a tolerance, not to another implementation bit for bit.
 #include <cuda_runtime.h>
 
 #include "common.cuh"

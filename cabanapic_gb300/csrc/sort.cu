@@ -13,12 +13,12 @@
 //               (atomics with return) and writes perm[slot] = its index
 //   4. gather:  particles[d] = copy[perm[d]], member by member (coalesced writes)
 // Passes 1 and 3 aggregate over the lanes of a warp that share a cell: one
-// atomic per cell per 32 particles.  Each warp takes kSortChunks chunks of 32 particles, all
-// loads and atomics issued before their results are used.  The order within
-// a cell depends on atomic arrival order.  The in-place
-// entry point gathers from a copy of the list in the scratch; the
-// out-of-place one (for callers with two lists) gathers straight into the
-// second list and skips that copy.
+// atomic per cell per 32 particles.  Each warp takes kSortChunks chunks of 32
+// particles, with all loads and atomics issued before their results are used.
+// The order within a cell depends on atomic arrival order.  The in-place entry
+// point gathers from a copy of the list in the scratch; the out-of-place one
+// (for callers with two lists) gathers straight into the second list and
+// skips that copy.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
