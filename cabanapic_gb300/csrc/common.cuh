@@ -155,15 +155,17 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
   return ok != 0;
 }
 // Warp-uniform wait for the completion of phase `parity` of mbarrier b.
-// Returns false, for the whole warp, after about 2^31 cycles (a second).
-__device__ __forceinline__ bool warp_wait(unsigned long long* b, unsigned parity) {
+// Returns false, for the whole warp, after `limit` cycles (by default 2^31,
+// about a second).
+__device__ __forceinline__ bool warp_wait(unsigned long long* b, unsigned parity,
+                                          long long limit = 1LL << 31) {
   bool done = mbar_try_wait(b, parity);
   if (__all_sync(kFull, done)) return true;
   const long long t0 = clock64();
   for (;;) {
     done = done || mbar_try_wait(b, parity);
     if (__all_sync(kFull, done)) return true;
-    const int late = (clock64() - t0) > (1LL << 31) ? 1 : 0;
+    const int late = (clock64() - t0) > limit ? 1 : 0;
     if (__shfl_sync(kFull, late, 0)) return false;
   }
 }

@@ -227,7 +227,28 @@ static bool bad_scratch(void* sc, size_t bytes) {
 
 using namespace cpic;
 
+// Self-test of the bounded device waits: one warp waits on phase 0 of a
+// shared-memory mbarrier that expects one arrival and gets none.  The wait
+// (the tiled push's warp_wait) gives up after `limit` cycles and the kernel
+// sets CPIC_STATUS_PIPELINE, as the push does when one of its waits gives up.
+// Nothing else is pending on the barrier, so the block then simply exits.
+__global__ void __launch_bounds__(32) bounded_wait_selftest_kernel(long long limit, int* __restrict__ status) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (!warp_wait(&bar, 0u, limit) && threadIdx.x == 0) atomicOr(status, CPIC_STATUS_PIPELINE);
+}
+
 extern "C" size_t cpic_diag_scratch_bytes(void) { return sizeof(DiagScratch); }
+
+extern "C" int cpic_selftest_bounded_wait(int64_t limit_cycles, int32_t* d_status, cpic_stream_t stream) {
+  // at most 2^31 cycles, the push's own limit
+  if (!d_status || ((uintptr_t)d_status & 3) || limit_cycles < 0 || limit_cycles > (1LL << 31))
+    return CPIC_EINVAL;
+  bounded_wait_selftest_kernel<<<1, 32, 0, reinterpret_cast<cudaStream_t>(stream)>>>((long long)limit_cycles,
+                                                                                   d_status);
+  return launch_status();
+}
 
 extern "C" int cpic_charge_density(const void* particles, int64_t num_particles, const cpic_grid* grid,
                                    int32_t precision, int32_t particle_vl, double qsp, double dx,

@@ -221,6 +221,14 @@ int cpic_particle_dump_values(const void* particles, int64_t num_particles, int3
 int cpic_field_dump_values(const void* fields, const cpic_grid* grid, int32_t precision, double xmin,
                            double dx, void* d_out, cpic_stream_t stream);
 
+/* ---------------------------------------------------------------- self-test
+ * Self-test of the bounded device waits (no counterpart in the reference):
+ * one warp waits on a shared-memory mbarrier phase that nothing completes,
+ * with the tiled push's wait loop; after `limit_cycles` GPU cycles
+ * (<= 2^31, the push's own limit) it gives up and OR-s
+ * CPIC_STATUS_PIPELINE into `d_status`.  The device stays usable. */
+int cpic_selftest_bounded_wait(int64_t limit_cycles, int32_t* d_status, cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- particle loading
  * Seeded uniform thermal plasma written on the device (no counterpart in the
  * reference, whose decks initialise particles on the host:

@@ -79,3 +79,32 @@ def test_reflect_boundary_rejected():
     with pytest.raises(capi.CpicError) as ei:
         pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Reflect)
     assert ei.value.code == capi.CPIC_EUNSUPPORTED
+
+
+def test_bounded_wait_gives_up_and_reports_the_pipeline_bit(orc):
+    """The tiled push's mbarrier wait, run on a barrier phase that nothing
+    completes, gives up after its cycle limit (here ~2^22 cycles, a few ms)
+    and sets CPIC_STATUS_PIPELINE; the context stays usable and the next
+    push is still exact."""
+    import time
+    from cabanapic_gb300 import capi, pic
+    status = pic.status_word()
+    pic.check_status()  # start clean
+    t0 = time.perf_counter()
+    capi.load().call("cpic_selftest_bounded_wait", 1 << 22, status.data_ptr(),
+                     torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert time.perf_counter() - t0 < 5.0
+    with pytest.raises(capi.CpicDeviceError) as ei:
+        pic.check_status()
+    assert ei.value.bits == capi.CPIC_STATUS_PIPELINE
+    assert capi.load().raw("cpic_selftest_bounded_wait")(1 << 40, status.data_ptr(), None) == capi.CPIC_EINVAL
+    # the device still works: an exact push matches the oracle bit for bit
+    st = random_state(n=3000, seed=14)
+    P, I, A = _setup(st)
+    host = st["particles"].copy()
+    acc = np.zeros((st["num_cells"], 3, 4), np.float32)
+    orc.push(host, st["n"], 32, st["interp"], *st["push_args"], acc, st["ogrid"])
+    pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic, exact=True)
+    pic.check_status()
+    assert np.array_equal(P.download_bytes(), host)
