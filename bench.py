@@ -175,7 +175,7 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
         host_packed, fields = decks.diocotron_state(deck, packed=True)
     # host_packed None: the thermal plasma is generated on the device (seeded
     # Philox, csrc/init.cu) and its initial state copied out for the other legs
-    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup,
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup + SORT_INTERVAL,
                      exact=exact, tiles=TILES, fields=fields)
     if host_packed is None:
         host_packed = sim.particles.download_bytes()
@@ -196,13 +196,50 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     push_ms = sim.push_times_ms()
+    # the step's phases, timed in one more sort interval after the timed
+    # region (so the timed steps carry only the push events)
+    sim.time_push = False
+    sim.time_phases = True
+    steps_before = sim.step_no
+    for _ in range(SORT_INTERVAL):
+        sim.step()
+    phases = sim.phase_times_ms()
+    phase_sort_steps = [k for k in range(len(phases)) if (steps_before + k) % SORT_INTERVAL == 0]
     sim.check_status()
     # timed steps that sorted first (step numbers count the warm-up steps)
     sort_steps = [k for k in range(steps) if (warmup + k) % SORT_INTERVAL == 0]
-    res = dict(ms=ms, push_ms=push_ms, deck=deck, energies=sim.energies(), sort_steps=sort_steps)
+    res = dict(ms=ms, push_ms=push_ms, deck=deck, energies=sim.energies(), sort_steps=sort_steps,
+               phases=phases, phase_sort_steps=phase_sort_steps)
     del sim
     torch.cuda.empty_cache()
     return res, host_packed
+
+
+def _phase_summary(res, deck, peak, steps):
+    """Mean CUDA-event times of the step's phases over one sort interval, the
+    field phase against its algorithmic bytes (324 B per ghosted cell: interp
+    96, clear 48, unload 60, 2x advance_b 72, advance_e 48) and the sort
+    amortised over the sort interval."""
+    ph = res["phases"]
+    mean = lambda k: float(np.mean([p[k] for p in ph]))
+    sorts = [p["sort"] for k, p in enumerate(ph) if k in res["phase_sort_steps"]]
+    field_ms = mean("interp_clear") + mean("field_solve")
+    field_bytes = 324 * deck.num_cells
+    achieved = field_bytes / (field_ms / 1e3) / 1e9
+    n = deck.num_particles
+    return {
+        "phases_ms": {"interp_clear": mean("interp_clear"), "push": mean("push"),
+                      "field_solve": mean("field_solve"),
+                      "sort_amortised": float(np.sum(sorts)) / len(ph) if sorts else 0.0},
+        "field_phase": {"ms": field_ms, "algorithmic_bytes": field_bytes, "achieved_gbs": achieved,
+                        "frac": achieved / peak,
+                        "basis": "324 B per ghosted cell: interp 96, clear 48, unload 60, 2x advance_b 72, "
+                                 "advance_e 48 (energies excluded)"},
+        "sort": {"ms_per_sort": float(np.mean(sorts)) if sorts else None, "sorts": len(sorts),
+                 "interval": SORT_INTERVAL, "bytes_per_particle_per_sort": 80,
+                 "achieved_gbs": (80 * n / (np.mean(sorts) / 1e3) / 1e9) if sorts else None,
+                 "amortised_bytes_per_particle_per_step": 80 / SORT_INTERVAL},
+    }
 
 
 def e2e_run(precision, steps, warmup, host_packed, ws):
@@ -378,8 +415,9 @@ def main():
         return
     traffic = _traffic_from_profiles()
     per_step_launches = 11  # interp, push, unload, 2x(advance_b + ghost copy), fold, ghost copy, advance_e, energies
-    # a sort adds rank, 3 scan passes, scatter and gather
+    # a sort adds count, 3 scan passes, scatter and gather
     launches = args.steps * per_step_launches + 6 * len(res["sort_steps"])
+    phases = _phase_summary(res, deck, peak, args.steps)
 
     exact = None
     if not args.no_exact:
@@ -432,6 +470,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes},
             "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "fp64": fp64, "exact": exact,
+            "phases_ms": phases["phases_ms"], "field_phase": phases["field_phase"], "sort": phases["sort"],
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -56,6 +56,8 @@ class Simulation:
         self.step_no = 0
         self.time_push = time_push
         self.push_events = []
+        self.time_phases = False  # events between the step's phases (phase_times_ms)
+        self.phase_events = []
         self.exact = bool(exact)
         self.tiles = bool(tiles)
         self.particle_dump = particle_dump
@@ -74,20 +76,31 @@ class Simulation:
     def step(self) -> None:
         d, p = self.deck, self.p
         nx, ny, nz, ng = d.nx, d.ny, d.nz, d.num_ghosts
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)] if self.time_phases else None
+        if ev:
+            ev[0].record()
         pic.load_interpolator_array(self.fields, self.interpolators, nx, ny, nz, ng, boundary=d.boundary)
         pic.clear_accumulator_array(self.fields, self.accumulators, nx, ny, nz)
-        if self.sorter is not None and self.step_no % self.sort_interval == 0:
+        if ev:
+            ev[1].record()
+        sorted_now = self.sorter is not None and self.step_no % self.sort_interval == 0
+        if sorted_now:
             self.sorter(self.particles)
-        if self.time_push:
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
+        if ev:
+            ev[2].record()
+        if self.time_push and not ev:
+            ev_push = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev_push[0].record()
         pic.push(self.particles, self.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
                  p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary, exact=self.exact,
                  tiles=self.tiles)
-        if self.time_push:
-            e1.record()
-            self.push_events.append((e0, e1))
+        if ev:
+            ev[3].record()
+            if self.time_push:
+                self.push_events.append((ev[2], ev[3]))
+        elif self.time_push:
+            ev_push[1].record()
+            self.push_events.append(ev_push)
         pic.unload_accumulator_array(self.fields, self.accumulators, nx, ny, nz, ng,
                                      p["dx"], p["dy"], p["dz"], p["dt"], boundary=d.boundary)
         half = d.R(0.5)
@@ -97,6 +110,9 @@ class Simulation:
         self.solver.advance_b(self.fields, hpx, hpy, hpz, nx, ny, nz, ng)
         if self.step_no < self.energy.shape[0]:
             self.solver.energies_async(self.fields, nx, ny, nz, ng, out=self.energy[self.step_no])
+        if ev:
+            ev[4].record()
+            self.phase_events.append((ev, sorted_now))
         if self._pdump is not None or self._fdump is not None:
             self.flush_dumps()
             if self._fdump is not None:
@@ -128,6 +144,17 @@ class Simulation:
     def energies(self) -> np.ndarray:
         """[steps, 2] history of (E, B) field energies, accumulated in double."""
         return self.energy[: min(self.step_no, self.energy.shape[0])].cpu().numpy()
+
+    def phase_times_ms(self) -> list:
+        """Per timed step: {"interp_clear", "sort" (0 when the step did not
+        sort), "push", "field_solve" (unload, advance_b/e/b, energies)} in ms."""
+        torch.cuda.synchronize()
+        out = []
+        for ev, sorted_now in self.phase_events:
+            out.append({"interp_clear": ev[0].elapsed_time(ev[1]),
+                        "sort": ev[1].elapsed_time(ev[2]) if sorted_now else 0.0,
+                        "push": ev[2].elapsed_time(ev[3]), "field_solve": ev[3].elapsed_time(ev[4])})
+        return out
 
     def push_times_ms(self) -> list:
         torch.cuda.synchronize()
