@@ -236,7 +236,7 @@ __device__ __forceinline__ R face_fraction(R dir, R p, R s) {
 // move_p for one particle (src/move_p.h:93-371), positions and displacement in
 // registers; writes the final offsets and cell of particle `pidx`.
 template <class R, int VL, bool FAST, class Acc>
-__device__ __noinline__ void move_one(unsigned char* __restrict__ part, R px, R py, R pz, R dx,
+__device__ __forceinline__ void move_one(unsigned char* __restrict__ part, R px, R py, R pz, R dx,
                                       R dy, R dz, R q, int cell, int pidx, Acc* __restrict__ acc,
                                       const GridDev g, int* __restrict__ status) {
   using L = PLayout<R, VL>;
