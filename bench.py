@@ -175,17 +175,17 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
         host_packed, fields = decks.diocotron_state(deck, packed=True)
     # host_packed None: the thermal plasma is generated on the device (seeded
     # Philox, csrc/init.cu) and its initial state copied out for the other legs
+    # graphs: steps that do not sort replay a captured graph of their launches
     sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup + SORT_INTERVAL,
-                     exact=exact, tiles=TILES, fields=fields)
+                     exact=exact, tiles=TILES, fields=fields, graphs=True)
     if host_packed is None:
         host_packed = sim.particles.download_bytes()
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
         sim.step()
+    sim.prepare_graphs()  # both particle buffers' graphs, before the timed region
     torch.cuda.synchronize()
     _barrier(ws)
-    sim.time_push = True
-    sim.push_events = []
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -195,15 +195,14 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    push_ms = sim.push_times_ms()
-    # the step's phases, timed in one more sort interval after the timed
-    # region (so the timed steps carry only the push events)
-    sim.time_push = False
+    # the push and the other phases, timed with events between them in one
+    # more sort interval after the timed region (launched eagerly there)
     sim.time_phases = True
     steps_before = sim.step_no
     for _ in range(SORT_INTERVAL):
         sim.step()
     phases = sim.phase_times_ms()
+    push_ms = [p["push"] for p in phases]
     phase_sort_steps = [k for k in range(len(phases)) if (steps_before + k) % SORT_INTERVAL == 0]
     sim.check_status()
     # timed steps that sorted first (step numbers count the warm-up steps)
@@ -257,9 +256,11 @@ def e2e_run(precision, steps, warmup, host_packed, ws):
     pinned_out = torch.empty_like(pinned_in).pin_memory()
     energies_host = torch.empty((steps, 2), dtype=torch.float64).pin_memory()
     # warm-up on the same arrays (not timed), then reset the state from the host
-    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup, tiles=TILES)
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup, tiles=TILES,
+                     graphs=True)
     for _ in range(warmup):
         sim.step()
+    sim.prepare_graphs()
     torch.cuda.synchronize()
     sim.step_no = 0
     stream = torch.cuda.current_stream()

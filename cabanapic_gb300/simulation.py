@@ -24,7 +24,7 @@ class Simulation:
     def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
                  max_steps: int = None, time_push: bool = False, exact: bool = False,
                  tiles: bool = True, fields=None, particle_dump=None, field_dump=None,
-                 acc_f64: bool = False):
+                 acc_f64: bool = False, graphs: bool = False):
         self.deck = deck
         self.p = deck.derived()
         dev = torch.device(device if device is not None else "cuda")
@@ -58,6 +58,14 @@ class Simulation:
         self.push_events = []
         self.time_phases = False  # events between the step's phases (phase_times_ms)
         self.phase_events = []
+        # graphs: a step that does not sort (and records no timing events and
+        # writes no dumps) replays a CUDA graph of its kernel launches, one
+        # graph per particle buffer (the sort alternates two); energies go
+        # to a fixed staging slot and are copied into the history
+        self.graphs = bool(graphs)
+        self._graphs = {}
+        self._warm = False  # one step launched eagerly (first-use setup done)
+        self._e_stage = torch.zeros(2, dtype=torch.float64, device=dev)
         self.exact = bool(exact)
         self.tiles = bool(tiles)
         self.particle_dump = particle_dump
@@ -76,14 +84,40 @@ class Simulation:
     def step(self) -> None:
         d, p = self.deck, self.p
         nx, ny, nz, ng = d.nx, d.ny, d.nz, d.num_ghosts
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)] if self.time_phases else None
+        sorted_now = self.sorter is not None and self.step_no % self.sort_interval == 0
+        dumps = self._pdump is not None or self._fdump is not None
+        if (self.graphs and self._warm and not sorted_now and not dumps and not self.time_push
+                and not self.time_phases):
+            self._graph(self.particles.buf).replay()
+            if self.step_no < self.energy.shape[0]:
+                self.energy[self.step_no].copy_(self._e_stage)
+        else:
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)] if self.time_phases else None
+            out = self.energy[self.step_no] if self.step_no < self.energy.shape[0] else None
+            self._launch_step(sorted_now, ev, out)
+            self._warm = True
+            if ev:
+                self.phase_events.append((ev, sorted_now))
+        if dumps:
+            self.flush_dumps()
+            if self._fdump is not None:
+                self._fdump.enqueue(self.fields, 0, p["dx"], nx, ny, nz, ng, d.boundary)
+            if self._pdump is not None:
+                self._pdump.enqueue(self.particles, 0, p["dx"], nx, ny, nz, ng, d.boundary)
+            self._pending_step = self.step_no + 1  # the reference's loop counts steps from 1
+        self.step_no += 1
+
+    def _launch_step(self, sorted_now: bool, ev, energy_out) -> None:
+        """The step's launches on the current stream (ev: 5 events between the
+        phases, or None; energy_out: the energies' device slot, or None)."""
+        d, p = self.deck, self.p
+        nx, ny, nz, ng = d.nx, d.ny, d.nz, d.num_ghosts
         if ev:
             ev[0].record()
         pic.load_interpolator_array(self.fields, self.interpolators, nx, ny, nz, ng, boundary=d.boundary)
         pic.clear_accumulator_array(self.fields, self.accumulators, nx, ny, nz)
         if ev:
             ev[1].record()
-        sorted_now = self.sorter is not None and self.step_no % self.sort_interval == 0
         if sorted_now:
             self.sorter(self.particles)
         if ev:
@@ -108,19 +142,39 @@ class Simulation:
         self.solver.advance_b(self.fields, hpx, hpy, hpz, nx, ny, nz, ng)
         self.solver.advance_e(self.fields, p["px"], p["py"], p["pz"], nx, ny, nz, ng, p["dt_eps0"])
         self.solver.advance_b(self.fields, hpx, hpy, hpz, nx, ny, nz, ng)
-        if self.step_no < self.energy.shape[0]:
-            self.solver.energies_async(self.fields, nx, ny, nz, ng, out=self.energy[self.step_no])
+        if energy_out is not None:
+            self.solver.energies_async(self.fields, nx, ny, nz, ng, out=energy_out)
         if ev:
             ev[4].record()
-            self.phase_events.append((ev, sorted_now))
-        if self._pdump is not None or self._fdump is not None:
-            self.flush_dumps()
-            if self._fdump is not None:
-                self._fdump.enqueue(self.fields, 0, p["dx"], nx, ny, nz, ng, d.boundary)
-            if self._pdump is not None:
-                self._pdump.enqueue(self.particles, 0, p["dx"], nx, ny, nz, ng, d.boundary)
-            self._pending_step = self.step_no + 1  # the reference's loop counts steps from 1
-        self.step_no += 1
+
+    def _graph(self, buf: torch.Tensor):
+        """The CUDA graph of a non-sorting step on particle buffer `buf`
+        (captured on first use; capturing launches nothing)."""
+        g = self._graphs.get(buf.data_ptr())
+        if g is None:
+            # first-use setup (shared-memory opt-in, occupancy, scratch)
+            # happens outside the capture, in an eager step
+            if not self._warm:
+                raise RuntimeError("graphs are captured after one eager step")
+            keep = self.particles.buf
+            self.particles.buf = buf
+            g = torch.cuda.CUDAGraph()
+            try:
+                with torch.cuda.graph(g):
+                    self._launch_step(False, None, self._e_stage)
+            finally:
+                self.particles.buf = keep
+            self._graphs[buf.data_ptr()] = g
+        return g
+
+    def prepare_graphs(self) -> None:
+        """Captures the step graphs of both particle buffers now (nothing is
+        launched), so that no capture happens inside a timed loop."""
+        if not self.graphs:
+            return
+        bufs = [self.particles.buf] + ([self.sorter.spare] if self.sorter is not None else [])
+        for b in bufs:
+            self._graph(b)
 
     def flush_dumps(self) -> None:
         """Writes the dumps enqueued at the last step (waits for their copies)."""
