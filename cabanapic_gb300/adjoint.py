@@ -56,10 +56,11 @@ class AdjointRun:
         self.K = 0
         self.timing = {}
         # device memory for the reverse sweep, allocated once: per step of a
-        # segment, the particles before the step and the step's interpolator
-        # array; the checkpoint buffers are kept and reused across runs
-        self._seg = [(torch.empty_like(self.sim.particles.buf), torch.empty_like(self.sim.interpolators.buf))
-                     for _ in range(self.C)]
+        # segment, the particles before the step (the first step's are the
+        # checkpoint's) and the step's interpolator array; the checkpoint
+        # buffers are kept and reused across runs
+        self._seg_P = [torch.empty_like(self.sim.particles.buf) for _ in range(self.C - 1)]
+        self._seg_I = [torch.empty_like(self.sim.interpolators.buf) for _ in range(self.C)]
         self._ck_bufs = []
 
     # ------------------------------------------------------------ forward
@@ -78,15 +79,23 @@ class AdjointRun:
         s.particles.buf.copy_(ck[0])
         s.fields.buf.copy_(ck[1])
 
-    def _step(self):
+    def _step(self, out: torch.Tensor = None, interp_only: bool = False):
+        """One forward step.  out: push out of place into this particle buffer
+        (the list keeps the state before the step); interp_only: stop after
+        the interpolator load."""
         s = self.sim
         d, p = s.deck, s.p
         nx, ny, nz, ng = d.nx, d.ny, d.nz, d.num_ghosts
         pic.load_interpolator_array(s.fields, s.interpolators, nx, ny, nz, ng)
+        if interp_only:
+            return
         pic.clear_accumulator_array(s.fields, s.accumulators, nx, ny, nz)
-        pic.push(s.particles, s.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
-                 p["qsp"], s.accumulators, None, nx, ny, nz, ng, d.boundary, true_sqrt=self.true_sqrt,
-                 exact=self.exact)
+        args = (s.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"], p["qsp"], s.accumulators,
+                None, nx, ny, nz, ng, d.boundary)
+        if out is None:
+            pic.push(s.particles, *args, true_sqrt=self.true_sqrt, exact=self.exact)
+        else:
+            pic.push_into(s.particles, out, *args, true_sqrt=self.true_sqrt, exact=self.exact)
         pic.unload_accumulator_array(s.fields, s.accumulators, nx, ny, nz, ng, p["dx"], p["dy"], p["dz"], p["dt"])
         h = d.R(0.5)
         s.solver.advance_b(s.fields, d.R(h * p["px"]), d.R(h * p["py"]), d.R(h * p["pz"]), nx, ny, nz, ng)
@@ -141,17 +150,27 @@ class AdjointRun:
         for seg in range(len(self.checkpoints) - 1, -1, -1):
             s0 = seg * self.C
             s1 = min(self.K, s0 + self.C)
-            self._restore(self.checkpoints[seg])
-            # per step of the segment: the particles before the step and the
-            # step's interpolator array (what the push adjoint reads; the
-            # field transposes are linear and need no forward state)
-            for n in range(s0, s1):
-                P, I = self._seg[n - s0]
-                P.copy_(self.sim.particles.buf)
-                self._step()
-                I.copy_(self.sim.interpolators.buf)
+            # recompute the segment, keeping per step the particles before the
+            # step and the step's interpolator array (what the push adjoint
+            # reads; the field transposes are linear and need no forward
+            # state).  Each push writes the next step's list out of place, the
+            # first reads the checkpoint's, and the last step needs only its
+            # interpolator array: nothing is copied.
+            ckP, ckF = self.checkpoints[seg]
+            sim = self.sim
+            sim.fields.buf.copy_(ckF)
+            keep = (sim.particles.buf, sim.interpolators.buf)
+            seg_P = [ckP] + self._seg_P
+            try:
+                for n in range(s0, s1):
+                    sim.particles.buf = seg_P[n - s0]
+                    sim.interpolators.buf = self._seg_I[n - s0]
+                    last = n + 1 == s1
+                    self._step(out=None if last else seg_P[n - s0 + 1], interp_only=last)
+            finally:
+                sim.particles.buf, sim.interpolators.buf = keep
             for n in range(s1 - 1, s0 - 1, -1):
-                P, I = self._seg[n - s0]
+                P, I = seg_P[n - s0], self._seg_I[n - s0]
                 lib.call("cpic_adjoint_advance_b", L.ptr, *hp, C.byref(grid), prec, stream)
                 lib.call("cpic_adjoint_advance_e", L.ptr, *fp, C.byref(grid), float(p["dt_eps0"]), prec, stream)
                 lib.call("cpic_adjoint_advance_b", L.ptr, *hp, C.byref(grid), prec, stream)

@@ -114,6 +114,8 @@ _SIGS = {
     "cpic_thermal_particles": (_i32, [_vp, _i64, _i32, C.POINTER(CpicGrid), _f64, _f64, C.c_uint64, _i32,
                                       _i32, _vp]),
     "cpic_selftest_bounded_wait": (_i32, [_i64, _vp, _vp]),
+    "cpic_push_into": (_i32, [_vp, _vp, _i64, _vp, _vp, C.POINTER(CpicGrid), C.POINTER(CpicPushParams), _vp,
+                              _vp]),
     "cpic_status_clear": (_i32, [_vp, _vp]),
     "cpic_status_read": (_i32, [_vp, _vp, C.POINTER(_i32)]),
 }

@@ -1,4 +1,5 @@
-// push.cu -- the exact push variant and the cpic_push entry point.
+// push.cu -- the exact push variant and the cpic_push / cpic_push_into entry
+// points.
 //
 // The kernel is in push_impl.cuh.  This translation unit is compiled with
 // --fmad=false (cabanapic_gb300/build.py) and instantiates it with IEEE
@@ -11,11 +12,13 @@ namespace cpic {
 // defined in push_fast.cu
 int push_fast_dispatch(void* particles, int n, const void* interp, void* acc, const cpic_grid* g,
                        const cpic_push_params* prm, int* status, cudaStream_t s);
+int push_into_fast_dispatch(const void* src, void* dst, int n, const void* interp, void* acc,
+                            const cpic_grid* g, const cpic_push_params* prm, int* status, cudaStream_t s);
 }  // namespace cpic
 
-extern "C" int cpic_push(void* particles, int64_t num_particles, const void* interpolators,
-                         void* accumulators, const cpic_grid* grid, const cpic_push_params* prm,
-                         int32_t* d_status, cpic_stream_t stream) {
+namespace {
+int check_push_args(int64_t num_particles, const cpic_grid* grid, const cpic_push_params* prm,
+                    const int32_t* d_status) {
   using namespace cpic;
   if (!grid || !prm || !d_status) return CPIC_EINVAL;
   int rc = check_grid(grid);
@@ -25,6 +28,16 @@ extern "C" int cpic_push(void* particles, int64_t num_particles, const void* int
   if (prm->particle_vl != 16 && prm->particle_vl != 32) return CPIC_EINVAL;
   if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT | CPIC_PUSH_STREAMING | CPIC_PUSH_ACC_F64))
     return CPIC_EINVAL;
+  return CPIC_OK;
+}
+}  // namespace
+
+extern "C" int cpic_push(void* particles, int64_t num_particles, const void* interpolators,
+                         void* accumulators, const cpic_grid* grid, const cpic_push_params* prm,
+                         int32_t* d_status, cpic_stream_t stream) {
+  using namespace cpic;
+  int rc = check_push_args(num_particles, grid, prm, d_status);
+  if (rc) return rc;
   if (num_particles == 0) return CPIC_OK;
   if (!particles || !interpolators || !accumulators) return CPIC_EINVAL;
   if (((uintptr_t)accumulators & 15) || ((uintptr_t)particles & 15) ||
@@ -36,4 +49,24 @@ extern "C" int cpic_push(void* particles, int64_t num_particles, const void* int
     return push_exact::push_dispatch<false>(particles, n, interpolators, accumulators, grid, prm,
                                             d_status, s);
   return push_fast_dispatch(particles, n, interpolators, accumulators, grid, prm, d_status, s);
+}
+
+extern "C" int cpic_push_into(const void* particles, void* out, int64_t num_particles,
+                              const void* interpolators, void* accumulators, const cpic_grid* grid,
+                              const cpic_push_params* prm, int32_t* d_status, cpic_stream_t stream) {
+  using namespace cpic;
+  int rc = check_push_args(num_particles, grid, prm, d_status);
+  if (rc) return rc;
+  if (prm->flags & CPIC_PUSH_STREAMING) return CPIC_EUNSUPPORTED;
+  if (num_particles == 0) return CPIC_OK;
+  if (!particles || !out || !interpolators || !accumulators || particles == out) return CPIC_EINVAL;
+  if (((uintptr_t)accumulators & 15) || ((uintptr_t)particles & 15) || ((uintptr_t)out & 15) ||
+      ((uintptr_t)interpolators & 15) || ((uintptr_t)d_status & 3))
+    return CPIC_EINVAL;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int n = (int)num_particles;
+  if (prm->flags & CPIC_PUSH_EXACT)
+    return push_exact::push_into_dispatch<false>(particles, out, n, interpolators, accumulators, grid, prm,
+                                                 d_status, s);
+  return push_into_fast_dispatch(particles, out, n, interpolators, accumulators, grid, prm, d_status, s);
 }

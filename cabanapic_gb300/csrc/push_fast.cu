@@ -15,4 +15,9 @@ int push_fast_dispatch(void* particles, int n, const void* interp, void* acc, co
   return push_fast::push_dispatch<true>(particles, n, interp, acc, g, prm, status, s);
 }
 
+int push_into_fast_dispatch(const void* src, void* dst, int n, const void* interp, void* acc,
+                            const cpic_grid* g, const cpic_push_params* prm, int* status, cudaStream_t s) {
+  return push_fast::push_into_dispatch<true>(src, dst, n, interp, acc, g, prm, status, s);
+}
+
 }  // namespace cpic

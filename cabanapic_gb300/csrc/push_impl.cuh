@@ -424,7 +424,7 @@ __device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, i
 // One 32-particle chunk: gather, Boris, in-cell move and deposit, queueing of
 // the crossers.  TILED gathers from the shared-memory window `wbuf` when the
 // particle's cell has a slot in window `w`.
-template <class R, int VL, bool LITERAL, bool FAST, bool TILED, class Acc>
+template <class R, int VL, bool LITERAL, bool FAST, bool TILED, class Acc, bool OUT = false>
 __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int n, int chunk,
                                            const PState<R>& cur, const R* __restrict__ interp,
                                            Acc* __restrict__ acc, const PushArgs<R>& a,
@@ -437,6 +437,7 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
   unsigned char* base = part + (size_t)chunk * kChunk;
   const int p = chunk * 32 + lc.lane;
   bool valid = p < n;
+  const bool inrange = valid;
   const R x = cur.x, y = cur.y, z = cur.z;
   R ux = cur.ux, uy = cur.uy, uz = cur.uz;
   int cell = cur.cell;
@@ -459,6 +460,16 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
     __stcs(reinterpret_cast<R*>(base + lc.lane_off + 3 * kMem), ux);
     __stcs(reinterpret_cast<R*>(base + lc.lane_off + 4 * kMem), uy);
     __stcs(reinterpret_cast<R*>(base + lc.lane_off + 5 * kMem), uz);
+    if constexpr (OUT) __stcs(reinterpret_cast<R*>(base + lc.lane_off + 6 * kMem), cur.w);
+  } else if (OUT && inrange) {  // a skipped particle is copied unchanged to the output list
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 0 * kMem), x);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 1 * kMem), y);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 2 * kMem), z);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 3 * kMem), cur.ux);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 4 * kMem), cur.uy);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 5 * kMem), cur.uz);
+    __stcs(reinterpret_cast<R*>(base + lc.lane_off + 6 * kMem), cur.w);
+    __stcs(reinterpret_cast<int*>(base + lc.lane_cell_off), cur.cell);
   }
 
   // normalised half displacement and the in-cell test (push.h:169-187)
@@ -474,6 +485,7 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
     __stcs(reinterpret_cast<R*>(base + lc.lane_off + 0 * kMem), nx);
     __stcs(reinterpret_cast<R*>(base + lc.lane_off + 1 * kMem), ny);
     __stcs(reinterpret_cast<R*>(base + lc.lane_off + 2 * kMem), nz);
+    if constexpr (OUT) __stcs(reinterpret_cast<int*>(base + lc.lane_cell_off), cell);
   }
   R v[12];
   const R corr = q * ux * uy * uz * one_third;
@@ -677,11 +689,14 @@ __device__ __forceinline__ int tile_sample(const unsigned char* __restrict__ par
 // their chunks of tile j gathering from the window, and arrive on
 // empty[j % 2].  No CTA-wide barrier: a warp delayed by a queue drain holds up
 // nobody until the producer needs its buffer again.
-template <class R, int VL, bool LITERAL, bool FAST, class Acc>
+// OUT: particles are read from `src` and written, all members, to the
+// same slots of `part` (a distinct list); otherwise `part` is pushed in place.
+template <class R, int VL, bool LITERAL, bool FAST, class Acc, bool OUT = false>
 __global__ void __launch_bounds__(kTiledThreads, sizeof(R) == 4 ? 2 : 1)  // FP32: 64 registers
 push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
                   Acc* __restrict__ acc, const PushArgs<R> a, int* __restrict__ status,
-                  int chunks_per_warp, int wxmax) {
+                  int chunks_per_warp, int wxmax, const unsigned char* __restrict__ src) {
+  const unsigned char* in = OUT ? src : part;
   constexpr size_t kChunk = (size_t)32 * (7 * sizeof(R) + sizeof(int));
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* const wbuf = reinterpret_cast<R*>(smem_raw);  // two windows of 9 * wxmax rows
@@ -707,8 +722,8 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
   __syncthreads();
 
   if (warp == 0) {  // ---------------------------------------- producer
-    int s_cur = tile_sample<R, VL>(part, n, T, blockIdx.x, lc.lane);
-    int s_nxt = (int)blockIdx.x + G < ntiles ? tile_sample<R, VL>(part, n, T, blockIdx.x + G, lc.lane) : 0;
+    int s_cur = tile_sample<R, VL>(in, n, T, blockIdx.x, lc.lane);
+    int s_nxt = (int)blockIdx.x + G < ntiles ? tile_sample<R, VL>(in, n, T, blockIdx.x + G, lc.lane) : 0;
     bool ok = true;
     int j = 0;
     for (int t = blockIdx.x; t < ntiles; t += G, ++j) {
@@ -719,7 +734,7 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
       }
       const TileWin w = window_from_samples(s_cur, lc.lane, wxmax, nc);
       s_cur = s_nxt;
-      if (t + 2 * G < ntiles) s_nxt = tile_sample<R, VL>(part, n, T, t + 2 * G, lc.lane);
+      if (t + 2 * G < ntiles) s_nxt = tile_sample<R, VL>(in, n, T, t + 2 * G, lc.lane);
       if (lc.lane == 0) wins[b] = w;
       stage_window<R>(wbuf + b * wrows, interp, w, ys, zs, nc, lc.lane);
       cp_async_mbar_arrive(&full[b]);
@@ -737,7 +752,7 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
   int t = blockIdx.x;
   int chunk = t * cpt + cw;
   PState<R> cur;
-  load_state<R, VL>(part + (size_t)chunk * kChunk, lc.lane_off, lc.lane_cell_off,
+  load_state<R, VL>(in + (size_t)chunk * kChunk, lc.lane_off, lc.lane_cell_off,
                     chunk < nchunks && chunk * 32 + lc.lane < n, cur);
   bool ok = true;
   for (int j = 0; t < ntiles; ++j, t += G) {
@@ -754,10 +769,10 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
       const bool last = i + 1 == chunks_per_warp;
       const int next = last ? t1 * cpt + cw : chunk + kConsumers;
       PState<R> nxt;
-      load_state<R, VL>(part + (size_t)next * kChunk, lc.lane_off, lc.lane_cell_off,
+      load_state<R, VL>(in + (size_t)next * kChunk, lc.lane_off, lc.lane_cell_off,
                         (!last || t1 < ntiles) && next < nchunks && next * 32 + lc.lane < n, nxt);
       if (chunk < nchunks)
-        push_chunk<R, VL, LITERAL, FAST, true, Acc>(part, n, chunk, cur, interp, acc, a, status, Q, qn,
+        push_chunk<R, VL, LITERAL, FAST, true, Acc, OUT>(part, n, chunk, cur, interp, acc, a, status, Q, qn,
                                                lc, wb, w, ys, zs);
       cur = nxt;
     }
@@ -813,10 +828,10 @@ inline TileShape tile_shape(const GridDev& g) {
   return ts;
 }
 
-template <class R, int VL, bool LITERAL, bool FAST, class Acc>
+template <class R, int VL, bool LITERAL, bool FAST, class Acc, bool OUT = false>
 int launch_push_tiled(void* particles, int n, const void* interp, void* acc, const PushArgs<R>& a,
-                      int* status, cudaStream_t s) {
-  auto kern = push_tiled_kernel<R, VL, LITERAL, FAST, Acc>;
+                      int* status, cudaStream_t s, const void* src = nullptr) {
+  auto kern = push_tiled_kernel<R, VL, LITERAL, FAST, Acc, OUT>;
   const TileShape ts = tile_shape(a.g);
   const size_t dyn = tiled_dyn_smem<R>(ts.wxmax);
   // Per device: the largest dynamic shared memory opted in so far (the
@@ -851,7 +866,8 @@ int launch_push_tiled(void* particles, int n, const void* interp, void* acc, con
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, kTiledThreads, dyn, s>>>(static_cast<unsigned char*>(particles), n,
                                                   static_cast<const R*>(interp), static_cast<Acc*>(acc), a,
-                                                  status, ts.chunks_per_warp, ts.wxmax);
+                                                  status, ts.chunks_per_warp, ts.wxmax,
+                                                  static_cast<const unsigned char*>(src));
   return launch_status();
 }
 
@@ -886,6 +902,33 @@ int push_dispatch(void* particles, int n, const void* interp, void* acc, const c
                    : launch_any<double, 32, false, FAST>(tiled, particles, n, interp, acc, a, status, s);
   return literal ? launch_any<double, 16, true, FAST>(tiled, particles, n, interp, acc, a, status, s)
                  : launch_any<double, 16, false, FAST>(tiled, particles, n, interp, acc, a, status, s);
+}
+
+// The out-of-place push (tiled kernel): particle p of `src` is pushed into
+// slot p of `dst`.
+template <bool FAST>
+int push_into_dispatch(const void* src, void* dst, int n, const void* interp, void* acc,
+                       const cpic_grid* g, const cpic_push_params* prm, int* status, cudaStream_t s) {
+  const bool literal = !(prm->flags & CPIC_PUSH_TRUE_SQRT);
+  const GridDev gd = make_grid(g);
+  if (gd.num_cells > (1 << 30)) return CPIC_EUNSUPPORTED;
+  if (prm->precision == CPIC_FLOAT) {
+    PushArgs<float> a{(float)prm->qdt_2mc, (float)prm->cdt_dx, (float)prm->cdt_dy,
+                      (float)prm->cdt_dz, (float)prm->qsp, gd};
+    if (prm->flags & CPIC_PUSH_ACC_F64)
+      return prm->particle_vl == 32
+                 ? launch_push_tiled<float, 32, true, FAST, double, true>(dst, n, interp, acc, a, status, s, src)
+                 : launch_push_tiled<float, 16, true, FAST, double, true>(dst, n, interp, acc, a, status, s, src);
+    return prm->particle_vl == 32
+               ? launch_push_tiled<float, 32, true, FAST, float, true>(dst, n, interp, acc, a, status, s, src)
+               : launch_push_tiled<float, 16, true, FAST, float, true>(dst, n, interp, acc, a, status, s, src);
+  }
+  PushArgs<double> a{prm->qdt_2mc, prm->cdt_dx, prm->cdt_dy, prm->cdt_dz, prm->qsp, gd};
+  if (prm->particle_vl == 32)
+    return literal ? launch_push_tiled<double, 32, true, FAST, double, true>(dst, n, interp, acc, a, status, s, src)
+                   : launch_push_tiled<double, 32, false, FAST, double, true>(dst, n, interp, acc, a, status, s, src);
+  return literal ? launch_push_tiled<double, 16, true, FAST, double, true>(dst, n, interp, acc, a, status, s, src)
+                 : launch_push_tiled<double, 16, false, FAST, double, true>(dst, n, interp, acc, a, status, s, src);
 }
 
 }  // namespace CPIC_PUSH_NS

@@ -83,7 +83,27 @@ def push(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy
     reciprocal square root (within 1e-5 relative per particle).  tiles=False
     selects the streaming kernel (no shared-memory cell windows; same
     results, slower once particles are in cell order)."""
-    lib = capi.load()
+    grid, prm = _push_args("cpic_push", particles, f0, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, a0, nx, ny,
+                           nz, num_ghosts, boundary, true_sqrt, exact, tiles)
+    capi.load().call("cpic_push", particles.ptr, particles.n, f0.ptr, a0.ptr, C.byref(grid), C.byref(prm),
+                     _STATUS.get().data_ptr(), _stream(stream))
+
+
+def push_into(particles: ParticleList, out, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp,
+              a0: AccumulatorArray, g, nx, ny, nz, num_ghosts, boundary, *, true_sqrt: bool = False,
+              exact: bool = False, stream=None) -> None:
+    """push() out of place (cpic_push_into): particle p of `particles` (left
+    unchanged) is pushed into slot p of `out` (a ParticleList or a device
+    buffer of the same size), every member written.  Tiled kernel."""
+    grid, prm = _push_args("cpic_push_into", particles, f0, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, a0, nx, ny,
+                           nz, num_ghosts, boundary, true_sqrt, exact, True)
+    dst = out.ptr if isinstance(out, ParticleList) else out.data_ptr()
+    capi.load().call("cpic_push_into", particles.ptr, dst, particles.n, f0.ptr, a0.ptr, C.byref(grid),
+                     C.byref(prm), _STATUS.get().data_ptr(), _stream(stream))
+
+
+def _push_args(fn, particles, f0, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, a0, nx, ny, nz, num_ghosts,
+               boundary, true_sqrt, exact, tiles):
     # an FP64 accumulator with FP32 particles: the compensated per-cell current sum
     acc_f64 = particles.precision == capi.CPIC_FLOAT and a0.precision == capi.CPIC_DOUBLE
     flags = ((capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0) | (capi.CPIC_PUSH_EXACT if exact else 0)
@@ -91,12 +111,11 @@ def push(particles: ParticleList, f0: InterpolatorArray, qdt_2mc, cdt_dx, cdt_dy
     prm = capi.CpicPushParams(float(qdt_2mc), float(cdt_dx), float(cdt_dy), float(cdt_dz),
                               float(qsp), particles.precision, particles.vl, flags, 0)
     if f0.precision != particles.precision or (a0.precision != particles.precision and not acc_f64):
-        raise capi.CpicError("cpic_push", capi.CPIC_EINVAL, "mixed real_t precisions")
+        raise capi.CpicError(fn, capi.CPIC_EINVAL, "mixed real_t precisions")
     grid = _grid(nx, ny, nz, num_ghosts, boundary)
     if f0.num_cells < grid_cells(nx, ny, nz, num_ghosts) or a0.num_cells < grid_cells(nx, ny, nz, num_ghosts):
-        raise capi.CpicError("cpic_push", capi.CPIC_EINVAL, "cell arrays smaller than the grid")
-    lib.call("cpic_push", particles.ptr, particles.n, f0.ptr, a0.ptr, C.byref(grid), C.byref(prm),
-             _STATUS.get().data_ptr(), _stream(stream))
+        raise capi.CpicError(fn, capi.CPIC_EINVAL, "cell arrays smaller than the grid")
+    return grid, prm
 
 
 def thermal_particles(particles: ParticleList, ppc: int, nx, ny, nz, uth: float, weight: float,

@@ -111,6 +111,15 @@ int cpic_push(void* particles, int64_t num_particles, const void* interpolators,
               void* accumulators, const cpic_grid* grid, const cpic_push_params* prm,
               int32_t* d_status, cpic_stream_t stream);
 
+/* The same push out of place: particle p of `particles` (not modified) is
+ * pushed into slot p of `out`, a distinct list of the same size, every member
+ * written.  For callers that keep the state before the step (the adjoint's
+ * segment recompute) without copying the list.  Tiled kernel only
+ * (CPIC_PUSH_STREAMING: CPIC_EUNSUPPORTED). */
+int cpic_push_into(const void* particles, void* out, int64_t num_particles, const void* interpolators,
+                   void* accumulators, const cpic_grid* grid, const cpic_push_params* prm,
+                   int32_t* d_status, cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- cells
  * Replaces: void load_interpolator_array(field_array_t fields,
  *   interpolator_array_t interpolators, size_t nx, ny, nz, ng)

@@ -81,6 +81,19 @@ def test_push_argument_validation(lib):
     assert push(dummy, 10, dummy, C.c_void_p(68), C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
 
 
+def test_push_into_argument_validation(lib):
+    from cabanapic_gb300 import capi
+    f = lib.raw("cpic_push_into")
+    g = capi.make_grid(4, 4, 4)
+    status = C.c_int32(0)
+    d, e = C.c_void_p(64), C.c_void_p(128)
+    assert f(d, e, 10, d, d, C.byref(g), C.byref(_prm(flags=capi.CPIC_PUSH_STREAMING)), C.byref(status), None) == capi.CPIC_EUNSUPPORTED
+    assert f(d, d, 10, d, d, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    assert f(d, None, 10, d, d, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    assert f(d, C.c_void_p(72), 10, d, d, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    assert f(None, None, 0, None, None, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_OK
+
+
 def test_field_argument_validation(lib):
     from cabanapic_gb300 import capi
     g = capi.make_grid(4, 4, 4)

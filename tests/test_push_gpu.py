@@ -205,3 +205,50 @@ def test_fp64_accumulation_bounds_hot_cell_error(orc, tiles):
     assert np.all(err32 <= 2 * 8192 / 32)  # the recursive-summation bound over the warp totals
     # the particle states are the same as with FP32 accumulators
     assert np.array_equal(P.download_bytes(), P32.download_bytes())
+
+
+@pytest.mark.parametrize("real,vl", [(np.float32, 32), (np.float32, 16), (np.float64, 32)])
+def test_push_into_matches_in_place_push(orc, real, vl):
+    """cpic_push_into: the out-of-place push writes exactly the in-place push's
+    particle bytes (all members, skipped particles copied unchanged) into the
+    second list and leaves the source untouched; the deposits agree within
+    the summation-order bound."""
+    from cabanapic_gb300 import layout as L, pic
+    st = random_state(nx=7, ny=6, nz=5, n=30011, seed=31, real=real, vl=vl, crossing=0.2, sort=True,
+                      disorder=0.2)
+    host = dict(st["host"])
+    host["cell"] = host["cell"].copy()
+    host["cell"][[3, 777]] = [-2, st["num_cells"] + 4]  # skipped and reported
+    packed = L.pack_particles(host, real, vl)
+    nc = st["num_cells"]
+    # the oracle (like the reference) has no range check: it pushes the two
+    # with valid cells and zero weight (no deposit), and the expected list
+    # then holds them unchanged
+    ok = {k: v.copy() for k, v in host.items()}
+    ok["cell"][[3, 777]] = st["host"]["cell"][[3, 777]]
+    ok["w"][[3, 777]] = 0
+    ref_p = L.pack_particles(ok, real, vl)
+    acc = np.zeros((nc, 3, 4), real)
+    acc_abs = np.zeros_like(acc)
+    cnt = np.zeros((nc, 3, 4), np.int32)
+    orc.push(ref_p, st["n"], vl, st["interp"], *st["push_args"], acc, st["ogrid"], acc_abs=acc_abs, acc_count=cnt)
+    out = L.unpack_particles(ref_p, st["n"], real, vl)
+    for k in out:
+        out[k][[3, 777]] = host[k][[3, 777]]
+    ref = L.pack_particles(out, real, vl)
+    P = pic.ParticleList(st["n"], real, vl).upload(packed)
+    Q = pic.ParticleList(st["n"], real, vl)
+    Q.buf.fill_(0xAB)
+    I = pic.InterpolatorArray(nc, real)
+    I.buf.copy_(torch.from_numpy(st["interp"]))
+    A = pic.AccumulatorArray(nc, real)
+    pic.push_into(P, Q, I, *st["push_args"], A, None, 7, 6, 5, 1, pic.Boundary.Periodic, exact=True)
+    with pytest.raises(Exception):
+        pic.check_status()  # the two out-of-range cells are reported
+    assert np.array_equal(P.download_bytes(), packed)
+    # every member of every particle (the padding slots of the last block are not written)
+    got, want = L.unpack_particles(Q.download_bytes(), st["n"], real, vl), L.unpack_particles(ref, st["n"], real, vl)
+    for k in want:
+        assert np.array_equal(got[k].view(np.uint8), want[k].view(np.uint8)), k
+    eps = np.finfo(real).eps
+    assert np.all(np.abs(A.get().astype(np.float64) - acc) <= reorder_bound(acc_abs, cnt, eps))
