@@ -327,3 +327,42 @@ def test_adjoint_interpolator_scatter_independent_of_particle_order():
     scale = np.abs(li_a).max()
     np.testing.assert_allclose(li_b, li_a, rtol=0, atol=1e-12 * scale)
     assert scale > 0
+
+
+@pytest.mark.parametrize("case", ["two-stream", "thermal3d"])
+def test_fp32_adjoint_matches_fp64_gpu_adjoint(case):
+    """The FP32 adjoint against the FP64 GPU adjoint of the same initial state
+    (the FP32 particles cast to FP64): the parameter gradients within 1e-3,
+    and the per-particle momentum adjoints within 1e-3 of their scale (all
+    but a few particles per thousand)."""
+    from cabanapic_gb300 import decks
+    from cabanapic_gb300.adjoint import AdjointRun, two_stream_drift_gradients
+    out = {}
+    for prec in (4, 8):
+        if case == "two-stream":
+            K = 40
+            d = decks.two_stream_1d(precision=prec, nx=32, ppc_per_beam=32, num_steps=K)
+            host = decks.two_stream_1d_particles(decks.two_stream_1d(precision=4, nx=32, ppc_per_beam=32))
+            host = {k: (v.astype(d.R) if k not in ("cell", "X", "sign") else v) for k, v in host.items()}
+            run = AdjointRun(d, host, checkpoint=10)
+            run.forward(K)
+            lam, _ = run.backward()
+            out[prec] = (np.array(two_stream_drift_gradients(lam, d, host)), lam["ux"].astype(np.float64))
+        else:
+            K = 12
+            d = decks.thermal(n=12, ppc=8, uth=0.1, dx=0.1, precision=prec, num_steps=K, seed=4)
+            host = decks.thermal_particles(decks.thermal(n=12, ppc=8, uth=0.1, dx=0.1, precision=4, seed=4))
+            host = {k: (v.astype(d.R) if k != "cell" else v) for k, v in host.items()}
+            f = np.zeros((d.num_cells, 9))
+            f[:, 0] = 0.02
+            run = AdjointRun(d, host, fields_init=f, checkpoint=5)
+            run.forward(K)
+            lam, lamF = run.backward()
+            a = lamF.reshape(d.nz + 2, d.ny + 2, d.nx + 2, 9)[1:-1, 1:-1, 1:-1]
+            out[prec] = (np.array([a[..., 0].sum()]), lam["ux"].astype(np.float64))
+    (g32, u32), (g64, u64) = out[4], out[8]
+    np.testing.assert_allclose(g32, g64, rtol=1e-3)
+    # a particle whose FP32 and FP64 runs cross a face at different steps has
+    # a different (piecewise constant) path: allow a few in a thousand
+    close = np.abs(u32 - u64) <= 1e-3 * np.abs(u64).max()
+    assert close.mean() >= 0.995, close.mean()
