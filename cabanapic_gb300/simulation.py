@@ -8,7 +8,10 @@ Energies are copied to the host on request.  With particle_dump / field_dump
 (open text files) the loop also writes the reference's per-step dumps
 (example.cpp:131-132, 273-277): each step's values are copied to pinned host
 memory asynchronously and written at the next step (or by flush_dumps()), so
-the copies overlap the following step's kernels.
+the copies overlap the following step's kernels.  With graphs=True, a step
+that does not sort replays a CUDA graph of its launches (captured once per
+particle buffer), removing the host launch overhead between the field phase's
+small kernels.
 """
 from __future__ import annotations
 
@@ -166,6 +169,11 @@ class Simulation:
                 self.particles.buf = keep
             self._graphs[buf.data_ptr()] = g
         return g
+
+    def reset_graphs(self) -> None:
+        """Drops the captured step graphs (they hold the launch configuration:
+        call this after changing exact, tiles or the arrays' buffers)."""
+        self._graphs = {}
 
     def prepare_graphs(self) -> None:
         """Captures the step graphs of both particle buffers now (nothing is
