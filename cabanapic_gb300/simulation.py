@@ -1,8 +1,8 @@
 """Time-loop driver: the per-step sequence of the reference's main()
 (example/example.cpp:216-271) on one GPU, through the C ABI.
 
-Each step: [cell sort every `sort_interval` steps] -> load_interpolator_array
--> clear_accumulator_array -> push -> unload_accumulator_array -> advance_b(1/2)
+Each step: load_interpolator_array -> clear_accumulator_array -> [cell sort
+every `sort_interval` steps] -> push -> unload_accumulator_array -> advance_b(1/2)
 -> advance_e -> advance_b(1/2) -> field energies (double, kept on the device).
 Energies are copied to the host on request.  With particle_dump / field_dump
 (open text files) the loop also writes the reference's per-step dumps
