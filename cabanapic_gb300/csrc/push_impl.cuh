@@ -821,8 +821,16 @@ struct TileShape {
   int chunks_per_warp, wxmax;
 };
 
+// 7 chunks per consumer warp (3,360 particles a tile) and windows of 44 voxels
+// per segment: 2 x (62 KB window buffers + 35 KB static) per SM stays inside
+// the 196 KB shared-memory carveout, which leaves 60 KB of L1.  At 64
+// particles per cell a tile spans ~52 voxels, so its edge cells (and every
+// cell at lower densities) gather from global memory; larger tiles amortise
+// the per-tile staging and measured faster than windows that cover the
+// whole tile (4 chunks and 36 voxels: 2.55 ms, 7 and 44: 2.47 ms at 128^3 x
+// 64 ppc; 48-voxel windows cross the carveout and cost 5%).
 inline TileShape tile_shape(const GridDev& g) {
-  TileShape ts{4, 36};
+  TileShape ts{7, 44};
   if (ts.wxmax > g.sx) ts.wxmax = g.sx;  // segments of one window must not overlap
   if (ts.wxmax < 3) ts.wxmax = 3;
   return ts;
