@@ -22,31 +22,30 @@
 //   cell order: a 13-shuffle reduce-scatter leaves 12 totals for 12 lanes,
 //   one atomic each), the other lanes use 16-byte vector reductions
 //   (red.global.add.v4.f32).
-//   push_tiled_kernel (default).  A CTA takes tiles of 32 * 7 * chunks_per_warp
-//   consecutive particles.  Once particles are in cell order a tile covers a
-//   short run of voxels [lo, hi]; its cell window is that run widened by one
-//   voxel on each side (the segment [c0, c0 + wx)) together with the eight
-//   segments offset by +-1 in y and z (strides sx, sx*sy): 9 segments, every
-//   cell a particle of the tile reaches some steps after a sort.  Warp 0 is a
-//   producer: it anchors each tile's window on the median of 32 sampled cells
-//   and stages the 18 interpolator coefficients of the window's cells in
-//   shared memory (rows of 20 values, 16-byte aligned) with cp.async, into two
-//   buffers handed over through mbarriers.  Warps 1..7 push the particles: a
-//   gather is five vector shared loads instead of 18 dependent global loads; a
+//   push_tiled_kernel (default).  A 512-thread CTA takes tiles of
+//   32 * 15 * chunks_per_warp consecutive particles.  Once particles are in
+//   cell order a tile covers a short run of voxels; its cell window is a
+//   segment of wx voxels [c0, c0 + wx) around that run together with the
+//   eight segments offset by +-1 in y and z (strides sx, sx*sy): 9 segments,
+//   the cells the tile's particles reach within a sort interval except the
+//   run's ends when the run is longer than the window.  Warp 0 is a producer:
+//   it anchors each tile's window on the median of 32 sampled cells and stages
+//   the 18 interpolator coefficients of the window's cells in shared memory
+//   (rows of 20 values, 16-byte aligned) with cp.async, into two buffers
+//   handed over through mbarriers.  Warps 1..15 push the particles: a gather
+//   is five vector shared loads instead of 18 dependent global loads; a
 //   particle whose cell has no slot gathers from global memory, so results do
-//   not depend on the order, only the speed does.  Deposits as in
-//   push_kernel.  (Measured and dropped: a shared accumulator window, since
+//   not depend on the order or the tile shape, only the speed does.  Deposits
+//   as in push_kernel.  (Measured and dropped: a shared accumulator window, since
 //   shared float atomics are compare-and-swap loops and the global reductions
 //   of reduced groups are cheap; and a CTA-wide barrier per tile in place of
 //   the producer warp, which cost a fifth of the warps' time in barrier stalls.)
 //
 // In both, cell-crossing particles are compacted into a per-warp shared-memory
-// queue (ballot + prefix popcount) holding the particle index and its
-// displacement; whenever 32 are queued the warp moves them together, so the
-// common path stays branch-free and the streak loop runs on full warps.  A
-// queued particle's offsets, weight and cell are still the ones in memory (an
-// in-cell particle's new offsets are stored, a crosser's are not) and are read
-// back when it is moved.  The streak loop is capped; hitting the cap sets
+// queue (ballot + prefix popcount) holding the particle's offsets, remaining
+// displacement, charge, cell and index; whenever 32 are queued the warp moves
+// them together, so the common path stays branch-free and the streak loop
+// runs on full warps.  The streak loop is capped; hitting the cap sets
 // CPIC_STATUS_MOVER_CAP.
 #pragma once
 
