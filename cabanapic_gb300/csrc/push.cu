@@ -59,7 +59,12 @@ extern "C" int cpic_push_into(const void* particles, void* out, int64_t num_part
   if (rc) return rc;
   if (prm->flags & CPIC_PUSH_STREAMING) return CPIC_EUNSUPPORTED;
   if (num_particles == 0) return CPIC_OK;
-  if (!particles || !out || !interpolators || !accumulators || particles == out) return CPIC_EINVAL;
+  if (!particles || !out || !interpolators || !accumulators) return CPIC_EINVAL;
+  {  // the two lists must not overlap
+    const uintptr_t bytes = (uintptr_t)cpic_particle_list_bytes(num_particles, prm->precision, prm->particle_vl);
+    const uintptr_t a0 = (uintptr_t)particles, b0 = (uintptr_t)out;
+    if (a0 < b0 + bytes && b0 < a0 + bytes) return CPIC_EINVAL;
+  }
   if (((uintptr_t)accumulators & 15) || ((uintptr_t)particles & 15) || ((uintptr_t)out & 15) ||
       ((uintptr_t)interpolators & 15) || ((uintptr_t)d_status & 3))
     return CPIC_EINVAL;

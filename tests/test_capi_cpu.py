@@ -89,6 +89,8 @@ def test_push_into_argument_validation(lib):
     d, e = C.c_void_p(64), C.c_void_p(128)
     assert f(d, e, 10, d, d, C.byref(g), C.byref(_prm(flags=capi.CPIC_PUSH_STREAMING)), C.byref(status), None) == capi.CPIC_EUNSUPPORTED
     assert f(d, d, 10, d, d, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
+    # overlapping lists (10 FP32 particles take one 1 KiB block)
+    assert f(C.c_void_p(4096), C.c_void_p(4096 + 512), 10, d, d, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
     assert f(d, None, 10, d, d, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
     assert f(d, C.c_void_p(72), 10, d, d, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
     assert f(None, None, 0, None, None, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_OK
