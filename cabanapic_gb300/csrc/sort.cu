@@ -305,7 +305,12 @@ extern "C" int cpic_sort_particles_into(const void* particles, void* sorted, int
   if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
   if (num_cells < 1 || num_cells > 0x7fffffffLL - 64) return CPIC_EINVAL;
   if (num_particles == 0) return CPIC_OK;
-  if (!particles || !sorted || !d_scratch || particles == sorted) return CPIC_EINVAL;
+  if (!particles || !sorted || !d_scratch) return CPIC_EINVAL;
+  {  // the two lists must not overlap
+    const uintptr_t bytes = (uintptr_t)cpic_particle_list_bytes(num_particles, precision, particle_vl);
+    const uintptr_t a0 = (uintptr_t)particles, b0 = (uintptr_t)sorted;
+    if (a0 < b0 + bytes && b0 < a0 + bytes) return CPIC_EINVAL;
+  }
   if (((uintptr_t)particles & 15) || ((uintptr_t)sorted & 15) || ((uintptr_t)d_scratch & 255))
     return CPIC_EINVAL;
   const SortPlan pl = plan_sort(num_particles, num_cells, precision, particle_vl);
