@@ -207,8 +207,9 @@ def test_fp64_accumulation_bounds_hot_cell_error(orc, tiles):
     assert np.array_equal(P.download_bytes(), P32.download_bytes())
 
 
-@pytest.mark.parametrize("real,vl", [(np.float32, 32), (np.float32, 16), (np.float64, 32)])
-def test_push_into_matches_in_place_push(orc, real, vl):
+@pytest.mark.parametrize("real,vl,acc64", [(np.float32, 32, False), (np.float32, 16, False), (np.float64, 32, False),
+                                            (np.float32, 32, True)])
+def test_push_into_matches_in_place_push(orc, real, vl, acc64):
     """cpic_push_into: the out-of-place push writes exactly the in-place push's
     particle bytes (all members, skipped particles copied unchanged) into the
     second list and leaves the source untouched; the deposits agree within
@@ -241,7 +242,7 @@ def test_push_into_matches_in_place_push(orc, real, vl):
     Q.buf.fill_(0xAB)
     I = pic.InterpolatorArray(nc, real)
     I.buf.copy_(torch.from_numpy(st["interp"]))
-    A = pic.AccumulatorArray(nc, real)
+    A = pic.AccumulatorArray(nc, np.float64 if acc64 else real)  # FP64 rows: CPIC_PUSH_ACC_F64
     pic.push_into(P, Q, I, *st["push_args"], A, None, 7, 6, 5, 1, pic.Boundary.Periodic, exact=True)
     with pytest.raises(Exception):
         pic.check_status()  # the two out-of-range cells are reported
