@@ -806,16 +806,13 @@ int launch_push(void* particles, int n, const void* interp, void* acc, const Pus
   return launch_status();
 }
 
-// Tile shape: 4 chunks per consumer warp (1920 particles).  Each tile sizes
-// its own window from its sampled cells (a run of 1920 / ppc voxels plus
-// margins), so the shape does not depend on the mean particle density, which
-// says little when particles fill part of the box; wxmax only bounds the
-// shared memory.  Two windows of 9 x 36 rows take 51.8 KB in FP32, 86.4 KB
-// per CTA with the 15 mover queues: two CTAs fit the 196 KB shared-memory
-// carveout and leave 60 KB of L1 (crossing into the 228 KB carveout, 28 KB of
-// L1, was measured 9% slower).  Runs longer than wxmax - 2 voxels (under ~57
-// particles per cell) get a window centred on the median sample and the rest
-// of the tile gathers from global memory.
+// Tile shape: chunks per consumer warp and the largest window segment.  Each
+// tile sizes its own window from its sampled cells (a run of tile / ppc
+// voxels plus margins), so the shape does not depend on the mean particle
+// density, which says little when particles fill part of the box; wxmax only
+// bounds the shared memory.  Runs longer than wxmax - 3 voxels get a window
+// centred on the median sample and the rest of the tile gathers from global
+// memory.
 struct TileShape {
   int chunks_per_warp, wxmax;
 };
