@@ -34,7 +34,7 @@ def _rank_main(rank, ws, port, out):
 def test_two_replicas_aggregate_with_gloo():
     ws = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_rank_main, args=(ws, port, out), nprocs=ws, join=True, start_method="spawn")
         res = dict(out)
