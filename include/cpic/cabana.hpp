@@ -9,7 +9,8 @@
 //
 // The containers here own device memory with the reference's byte layouts
 // (layout.h).  A Kokkos/Cabana build would instead pass its own views'
-// .data() pointers to the cpic_* functions directly.
+// .data() pointers to the cpic_* functions directly, from the bodies of its
+// push() and field functions.
 // Errors: a non-zero C-ABI return code throws cpic::Error.
 #pragma once
 
