@@ -1,7 +1,7 @@
 // cpic_oracle.cpp -- CPU restatement of CabanaPIC's per-step hot path.
 //
 // TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: the tests, the
-// smoke check and the CPU-baseline leg of the benchmark load it as the checker.
+// smoke check and the CPU-baseline leg of the benchmark load it as the oracle.
 // Nothing in the shipped library (cabanapic_gb300/) links, loads or calls it.
 //
 // Parity pin: the oracle reproduces the reference's own golden energy histories

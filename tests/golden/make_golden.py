@@ -2,8 +2,8 @@
 
 The reference's only regression data for this path are the 2stream-em energy
 histories (tests/energy_comparison/energies_gold.2stream-em.{float,double} in
-the reference tree: 6000 rows of `step time E B`).  The GPU machine does not have
-the reference tree, so the fixtures are committed; this script regenerates
+the reference tree: 6000 rows of `step time E B`).  The machines that run the
+GPU tests do not have the reference tree, so the fixtures are committed; this script regenerates
 them from a checkout of the reference.
 
 usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
