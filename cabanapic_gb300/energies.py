@@ -1,8 +1,10 @@
 """energies.txt: the reference's energy-history format and its comparison rule.
 
-write_history / append_line produce `step time E B` lines as dump_energies
-does (src/fields.h:722-763: a std::ostream at its default 6-significant-digit
-precision, one line per step, steps from 1).  compare_files applies the rule of
+energy_line / write_history produce the `step time E B` lines that
+dump_energies writes to energies.txt (src/fields.h:722-763: a std::ostream at
+its default 6-significant-digit precision, one line per step, steps from 1);
+stdout_line is the line it prints to stdout at the same time (printf
+"%d %f %e %e"), the format of the reference's gold energy files.  compare_files applies the rule of
 the reference's regression test (tests/energy_comparison/compare_energies.h:
 69-106, 135-362, as called by 2stream-em.cxx:45-70): skip N lines, then for M
 lines sum the masked tokens (bit k selects token k, token 0 = step) and
@@ -30,14 +32,20 @@ def energy_line(step: int, time: float, e: float, b: float) -> str:
     return f"{step} {_fmt(time)} {_fmt(e)} {_fmt(b)}"
 
 
-def history_lines(energies: Sequence[Sequence[float]], dt: float, first_step: int = 1) -> List[str]:
-    return [energy_line(first_step + i, (first_step + i) * dt, float(r[0]), float(r[1]))
+def stdout_line(step: int, time: float, e: float, b: float) -> str:
+    return f"{step} {time:f} {e:e} {b:e}"
+
+
+def history_lines(energies: Sequence[Sequence[float]], dt: float, first_step: int = 1,
+                  stdout_format: bool = False) -> List[str]:
+    fmt = stdout_line if stdout_format else energy_line
+    return [fmt(first_step + i, (first_step + i) * dt, float(r[0]), float(r[1]))
             for i, r in enumerate(energies)]
 
 
-def write_history(path: str, energies, dt: float, first_step: int = 1) -> None:
+def write_history(path: str, energies, dt: float, first_step: int = 1, stdout_format: bool = False) -> None:
     with open(path, "w") as fh:
-        for line in history_lines(energies, dt, first_step):
+        for line in history_lines(energies, dt, first_step, stdout_format):
             fh.write(line + "\n")
 
 

@@ -327,7 +327,8 @@ inline void dump_particles(FILE* fp, const particle_list_t& particles, const rea
 }
 
 // dump_energies, src/fields.h:722-763: appends `step time E B` to energies.txt
-// (truncating at step 0), std::ostream default formatting.
+// (truncating at step 0), std::ostream default formatting, and prints the same
+// line to stdout as printf("%d %f %e %e\n") does there.
 #include <fstream>
 template <typename field_solver_t>
 void dump_energies(field_solver_t& field_solver, field_array_t& fields, int step, real_t time,
@@ -339,4 +340,5 @@ void dump_energies(field_solver_t& field_solver, field_array_t& fields, int step
   if (step == 0) f.open(path, std::ofstream::out | std::ofstream::trunc);
   else f.open(path, std::ios::app);
   f << step << " " << time << " " << e_en << " " << b_en << std::endl;
+  printf("%d %f %e %e\n", step, (double)time, e_en, b_en);
 }

@@ -1,0 +1,91 @@
+"""The energy-history text formats against the C and C++ libraries that write
+them in the reference (src/fields.h:722-763): energies.txt through a
+std::ostream at its default precision (energy_line), and the stdout line of
+printf("%d %f %e %e\\n") (stdout_line), which is the format of the
+reference's gold files.  A small g++ program prints both for the same values."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from cabanapic_gb300 import energies as E
+from conftest import gold_path
+
+_CPP = r"""
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+int main(int argc, char** argv) {
+  // stdin: step time e b per line; stdout: the ostream line, then the printf line
+  int step; double t, e, b;
+  while (std::scanf("%d %lf %lf %lf", &step, &t, &e, &b) == 4) {
+    std::cout << step << " " << t << " " << e << " " << b << std::endl;
+    std::printf("%d %f %e %e\n", step, t, e, b);
+    std::fflush(stdout);
+  }
+  return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def cpp_format(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("fmt")
+    src, exe = d / "fmt.cpp", d / "fmt"
+    src.write_text(_CPP)
+    subprocess.run([gxx, "-O1", "-o", str(exe), str(src)], check=True)
+
+    def run(rows):
+        inp = "".join(f"{s} {t!r} {e!r} {b!r}\n" for s, t, e, b in rows)
+        out = subprocess.run([str(exe)], input=inp, capture_output=True, text=True, check=True).stdout
+        lines = out.splitlines()
+        return lines[0::2], lines[1::2]
+
+    return run
+
+
+def _rows():
+    rng = np.random.default_rng(5)
+    mags = 10.0 ** rng.uniform(-120, 120, 300)
+    vals = list(mags * rng.choice([-1, 1], 300)) + [0.0, 1.0, 0.1, 1e-5, 123456.5, 1234567.0, 0.0001,
+                                                     9.9999995e-5, 2.5e100, 1e-300]
+    rows = []
+    for i, v in enumerate(vals):
+        rows.append((i, 0.019549 * i, float(v), float(abs(v) * 0.37 + 1e-20)))
+    return rows
+
+
+def test_ostream_and_printf_lines_match_the_c_libraries(cpp_format):
+    rows = _rows()
+    ostream, printf = cpp_format(rows)
+    assert len(ostream) == len(rows) == len(printf)
+    for (s, t, e, b), lo, lp in zip(rows, ostream, printf):
+        assert E.energy_line(s, t, e, b) == lo
+        assert E.stdout_line(s, t, e, b) == lp
+
+
+@pytest.mark.parametrize("kind", ["float", "double"])
+def test_stdout_line_reproduces_the_gold_files(kind):
+    lines = open(gold_path(kind)).read().splitlines()
+    assert len(lines) == 6000
+    for ln in lines:
+        s, t, e, b = ln.split(" ")
+        assert E.stdout_line(int(s), float(t), float(e), float(b)) == ln
+
+
+def test_history_in_either_format_passes_the_rule_against_gold(tmp_path):
+    from cabanapic_gb300 import decks
+    g = np.loadtxt(gold_path("double"))
+    dt = decks.two_stream_em(precision=8).dt
+    for fmt in (False, True):
+        path = tmp_path / f"e{int(fmt)}.txt"
+        E.write_history(str(path), g[:, 2:4], dt, first_step=0, stdout_format=fmt)
+        (e_ok, e_err, _), (b_ok, b_err, _) = E.two_stream_em_rule(gold_path("double"), str(path))
+        assert e_ok and b_ok and e_err < 1e-5 and b_err < 1e-5
+    # the stdout format with the deck's dt rewrites the gold file byte for byte
+    assert open(tmp_path / "e1.txt").read() == open(gold_path("double")).read()
