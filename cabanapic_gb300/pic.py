@@ -16,7 +16,7 @@ import os
 import numpy as np
 import torch
 
-from . import capi
+from . import capi, energies as _energies
 from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleList
 
 
@@ -267,26 +267,18 @@ class ESFieldSolver1D:
 
 
 def dump_energies(field_solver: EMFieldSolver, fields: FieldArray, step, time, px, py, pz, nx, ny,
-                  nz, ng, path: str = "energies.txt") -> tuple:
-    """dump_energies (src/fields.h:722-763): appends `step time E B` (truncates at step 0)."""
+                  nz, ng, path: str = "energies.txt", echo: bool = True) -> tuple:
+    """dump_energies (src/fields.h:722-763): appends the `step time E B` line
+    to `path` in std::ostream format (truncating the file at step 0) and, as
+    the reference does, prints the printf("%d %f %e %e") line to stdout
+    (echo=False leaves stdout alone).  Returns (E, B)."""
     e, b = field_solver.energies_async(fields, nx, ny, nz, ng).cpu().tolist()
     mode = "w" if step == 0 else "a"
     with open(path, mode) as fh:
-        fh.write(_energy_line(step, time, e, b) + "\n")
+        fh.write(_energies.energy_line(step, time, e, b) + "\n")
+    if echo:
+        print(_energies.stdout_line(step, time, e, b), flush=True)
     return e, b
-
-
-def _g6(v: float) -> str:
-    s = f"{v:.6g}"
-    if "e" in s:
-        mant, exp = s.split("e")
-        digits = exp[1:].lstrip("0") or "0"
-        s = f"{mant}e{exp[0]}{digits.zfill(2)}"
-    return s
-
-
-def _energy_line(step, time, e, b) -> str:
-    return f"{step} {_g6(time)} {_g6(e)} {_g6(b)}"
 
 
 # ---------------------------------------------------------------- dumps

@@ -89,3 +89,33 @@ def test_history_in_either_format_passes_the_rule_against_gold(tmp_path):
         assert e_ok and b_ok and e_err < 1e-5 and b_err < 1e-5
     # the stdout format with the deck's dt rewrites the gold file byte for byte
     assert open(tmp_path / "e1.txt").read() == open(gold_path("double")).read()
+
+
+def test_pic_dump_energies_writes_the_file_and_echoes_the_stdout_line(tmp_path, capsys):
+    """pic.dump_energies over a stand-in solver (the energies come from the
+    device in real runs): truncates at step 0, appends after, and prints the
+    reference's stdout line."""
+    torch = pytest.importorskip("torch")
+    from cabanapic_gb300 import pic
+
+    vals = {0: (8.973809e-13, 8.449903e-15), 1: (3.455599e-12, 1.326642e-13), 2: (7.283853e-12, 6.504499e-13)}
+
+    class Solver:
+        step = 0
+
+        def energies_async(self, fields, nx, ny, nz, ng):
+            return torch.tensor(vals[self.step], dtype=torch.float64)
+
+    path = tmp_path / "energies.txt"
+    path.write_text("stale\n")
+    s = Solver()
+    dt = 0.0195487
+    for k in range(3):
+        s.step = k
+        pic.dump_energies(s, None, k, k * dt, 0, 0, 0, 4, 4, 4, 1, path=str(path))
+    assert path.read_text().splitlines() == [E.energy_line(k, k * dt, *vals[k]) for k in range(3)]
+    assert capsys.readouterr().out.splitlines() == [E.stdout_line(k, k * dt, *vals[k]) for k in range(3)]
+    s.step = 0
+    pic.dump_energies(s, None, 0, 0.0, 0, 0, 0, 4, 4, 4, 1, path=str(path), echo=False)
+    assert path.read_text().splitlines() == [E.energy_line(0, 0.0, *vals[0])]
+    assert capsys.readouterr().out == ""
