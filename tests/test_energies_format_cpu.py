@@ -2,7 +2,8 @@
 them in the reference (src/fields.h:722-763): energies.txt through a
 std::ostream at its default precision (energy_line), and the stdout line of
 printf("%d %f %e %e\\n") (stdout_line), which is the format of the
-reference's gold files.  A small g++ program prints both for the same values."""
+reference's gold files.  A small g++ program prints both for the same values.
+The particle and field dump lines are checked against C printf the same way."""
 import os
 import shutil
 import subprocess
@@ -119,3 +120,38 @@ def test_pic_dump_energies_writes_the_file_and_echoes_the_stdout_line(tmp_path, 
     pic.dump_energies(s, None, 0, 0.0, 0, 0, 0, 4, 4, 4, 1, path=str(path), echo=False)
     assert path.read_text().splitlines() == [E.energy_line(0, 0.0, *vals[0])]
     assert capsys.readouterr().out == ""
+
+
+_CPP_PAIRS = r"""
+#include <cstdio>
+int main() {
+  // stdin: pairs of floats; stdout: the particle dump's "%e  %e " per pair,
+  // a newline, then the field dump's "%e %e\n" per pair
+  static float v[4096];
+  int n = 0;
+  while (n < 4096 && std::scanf("%f", &v[n]) == 1) ++n;
+  for (int i = 0; i + 1 < n; i += 2) std::printf("%e  %e ", v[i], v[i + 1]);
+  std::printf("\n");
+  for (int i = 0; i + 1 < n; i += 2) std::printf("%e %e\n", v[i], v[i + 1]);
+  return 0;
+}
+"""
+
+
+def test_dump_pairs_match_c_printf(tmp_path):
+    """The particle and field dump lines (fprintf "%e  %e " and "%e %e\\n" of
+    real_t values in the reference) from FP32 values, against C printf."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    from cabanapic_gb300 import pic
+    src, exe = tmp_path / "pairs.cpp", tmp_path / "pairs"
+    src.write_text(_CPP_PAIRS)
+    subprocess.run([gxx, "-O1", "-o", str(exe), str(src)], check=True)
+    rng = np.random.default_rng(9)
+    v = (rng.standard_normal(400) * 10.0 ** rng.uniform(-30, 30, 400)).astype(np.float32)
+    v[:4] = [0.0, -0.0, 1.0, -3.5]
+    inp = " ".join(repr(float(x)) for x in v)
+    out = subprocess.run([str(exe)], input=inp, capture_output=True, text=True, check=True).stdout
+    expect = pic._fmt_pairs(v, "  ", " ") + "\n" + pic._fmt_pairs(v, " ", "\n")
+    assert out == expect
