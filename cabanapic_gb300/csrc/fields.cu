@@ -595,24 +595,19 @@ extern "C" int cpic_field_energies(const void* fields, const cpic_grid* grid, in
 static_assert(sizeof(EnergyScratch) == 9480, "static energy scratch size is documented as 9,480 bytes");
 static __device__ __align__(256) EnergyScratch g_energy_noalloc_scratch;
 
-constexpr int kMaxDevices = 64;
-// Device address of g_energy_noalloc_scratch per device.  The array's name in
-// host code is only a host-side stand-in, so the address is looked up once per
-// device (by the first call on that device, with it current).
-static std::atomic<EnergyScratch*> g_energy_noalloc_addr[kMaxDevices];
-
+// Device address of g_energy_noalloc_scratch in the current device's context.
+// The array's name in host code is only a host-side stand-in, so the address
+// is looked up with that device current, on every call: a cached address
+// would go stale if the context were destroyed and recreated (for example by
+// cudaDeviceReset), which reloads the module, possibly elsewhere.  Once the
+// module is loaded the lookup is a host-side table read.  The first call on a
+// device may load the module (lazy loading), which is why that first call
+// should come before any stream capture.
 static EnergyScratch* energy_noalloc_scratch() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
-  EnergyScratch* p = g_energy_noalloc_addr[dev].load(std::memory_order_acquire);
-  if (p == nullptr) {
-    void* addr = nullptr;
-    if (cudaGetSymbolAddress(&addr, g_energy_noalloc_scratch) != cudaSuccess || addr == nullptr)
-      return nullptr;
-    p = static_cast<EnergyScratch*>(addr);
-    g_energy_noalloc_addr[dev].store(p, std::memory_order_release);
-  }
-  return p;
+  void* addr = nullptr;
+  if (cudaGetSymbolAddress(&addr, g_energy_noalloc_scratch) != cudaSuccess || addr == nullptr)
+    return nullptr;
+  return static_cast<EnergyScratch*>(addr);
 }
 
 extern "C" int cpic_field_energies_noalloc(const void* fields, const cpic_grid* grid,

@@ -183,9 +183,11 @@ int cpic_field_energies(const void* fields, const cpic_grid* grid, int32_t preci
  * (592 block partial sums and a completion counter; every GPU that loads the
  * library keeps it until exit).  The scratch need does not grow with the grid;
  * grids beyond the library's limits (an axis above 2^20 cells, 2^31 ghosted
- * cells or more) return CPIC_EINVAL.  The first call on a device looks up the
- * array's device address, so make that first call before any stream capture.
- * All calls share the one array: calls that overlap on the GPU (concurrent
+ * cells or more) return CPIC_EINVAL.  Every call looks up the array's device
+ * address in the current device's context (so a context recreated after
+ * cudaDeviceReset is served correctly); the first call on a device may load
+ * the library's device code, so make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU (concurrent
  * streams) race and must be serialised by the caller. */
 int cpic_field_energies_noalloc(const void* fields, const cpic_grid* grid, int32_t precision,
                                 double* d_out, cpic_stream_t stream);
