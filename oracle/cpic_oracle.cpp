@@ -582,6 +582,59 @@ void default_particle_init(const Particles<R>& P, size_t n, size_t nx, size_t ny
 // Parameters of a run, as _Input_Deck holds them after derive_params()
 // (src/input/deck.h:254-348) plus the constants main() derives
 // (example/example.cpp:77-113,179-181).
+// Seeded uniform thermal plasma (the thermal deck's loader, restated from
+// cabanapic_gb300/decks.py thermal_particles; no counterpart in the reference,
+// whose decks initialise particles on the host: src/input/deck.h:79-158).
+// Particle p in interior cell p / ppc (VOXEL order, x fastest) draws from
+// Philox4x32-10 (Salmon et al., SC'11) at counters (p, 0) and (p, 1) under
+// the 64-bit seed: offsets 2u - 1, momenta Box-Muller normals in double
+// rounded once to real_t.  OpenMP over particles; used to make the CPU
+// baseline's inputs quickly.
+struct U4 { uint32_t x, y, z, w; };
+
+static U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)c.x * 0xD2511F53u, p1 = (uint64_t)c.z * 0xCD9E8D57u;
+    c = U4{(uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+template <class R>
+static R thermal_offset(uint32_t r) {
+  if constexpr (sizeof(R) == 4) return (float)(r >> 8) * 0x1p-23f - 1.0f;
+  else return (double)r * 0x1p-31 - 1.0;
+}
+
+template <class R>
+void thermal_particles(const Particles<R>& P, size_t n, long ppc, long nx, long ny, double uth, R weight,
+                       uint64_t seed) {
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const long sx = nx + 2, sy = ny + 2;
+  const double pi = 3.14159265358979323846;
+#pragma omp parallel for schedule(static)
+  for (long p = 0; p < (long)n; ++p) {
+    const long k = p / ppc;
+    const long ix = k % nx, iy = (k / nx) % ny, iz = k / (nx * ny);
+    const U4 a = philox4x32_10(U4{(uint32_t)p, (uint32_t)((uint64_t)p >> 32), 0u, 0u}, k0, k1);
+    const U4 b = philox4x32_10(U4{(uint32_t)p, (uint32_t)((uint64_t)p >> 32), 1u, 0u}, k0, k1);
+    const double r1 = std::sqrt(-2.0 * std::log(((double)a.w + 1.0) * 0x1p-32));
+    const double r2 = std::sqrt(-2.0 * std::log(((double)b.y + 1.0) * 0x1p-32));
+    const double t1 = pi * (2.0 * ((double)b.x * 0x1p-32));
+    const double t2 = pi * (2.0 * ((double)b.z * 0x1p-32));
+    P.mem(0, p) = thermal_offset<R>(a.x);
+    P.mem(1, p) = thermal_offset<R>(a.y);
+    P.mem(2, p) = thermal_offset<R>(a.z);
+    P.mem(3, p) = (R)(uth * (r1 * std::cos(t1)));
+    P.mem(4, p) = (R)(uth * (r1 * std::sin(t1)));
+    P.mem(5, p) = (R)(uth * (r2 * std::cos(t2)));
+    P.mem(6, p) = weight;
+    P.cell(p) = (int)((ix + 1) + sx * ((iy + 1) + sy * (iz + 1)));
+  }
+}
+
 template <class R>
 struct Run {
   size_t nx, ny, nz, ng, nppc, num_particles, num_cells;
@@ -789,6 +842,20 @@ int orc_uncenter_f32(void* particles, int64_t n, int32_t vl, const float* interp
 int orc_uncenter_f64(void* particles, int64_t n, int32_t vl, const double* interp, double qdt_2mc) {
   orc::Particles<double> P{(unsigned char*)particles, vl};
   orc::uncenter<double>(P, (size_t)n, interp, qdt_2mc);
+  return 0;
+}
+
+int orc_thermal_particles_f32(void* particles, int64_t n, int32_t vl, int64_t ppc, int64_t nx, int64_t ny,
+                              double uth, float weight, uint64_t seed) {
+  orc::Particles<float> P{(unsigned char*)particles, vl};
+  orc::thermal_particles<float>(P, (size_t)n, (long)ppc, (long)nx, (long)ny, uth, weight, seed);
+  return 0;
+}
+
+int orc_thermal_particles_f64(void* particles, int64_t n, int32_t vl, int64_t ppc, int64_t nx, int64_t ny,
+                              double uth, double weight, uint64_t seed) {
+  orc::Particles<double> P{(unsigned char*)particles, vl};
+  orc::thermal_particles<double>(P, (size_t)n, (long)ppc, (long)nx, (long)ny, uth, weight, seed);
   return 0;
 }
 

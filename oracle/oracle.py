@@ -56,6 +56,8 @@ class Oracle:
         lib.orc_uncenter_f32.argtypes = [_c_p, _i64, _i32, _c_p, _f32]
         lib.orc_uncenter_f64.argtypes = [_c_p, _i64, _i32, _c_p, _f64]
         lib.orc_num_threads.restype = _i32
+        lib.orc_thermal_particles_f32.argtypes = [_c_p, _i64, _i32, _i64, _i64, _i64, _f64, _f32, C.c_uint64]
+        lib.orc_thermal_particles_f64.argtypes = [_c_p, _i64, _i32, _i64, _i64, _i64, _f64, _f64, C.c_uint64]
 
     @staticmethod
     def grid(nx, ny, nz, ng=1) -> OrcGrid:
@@ -134,6 +136,18 @@ class Oracle:
             raise RuntimeError(f"orc_run_two_stream_em failed: {rc}")
         keys = ["dt", "dx", "dy", "dz", "qdt_2mc", "we", "len_y", "py"]
         return out, dict(zip(keys, params.tolist()))
+
+    def thermal_particles(self, deck) -> np.ndarray:
+        """The thermal deck's particles (decks.thermal_particles restated in
+        C with OpenMP, for large CPU baselines): packed AoSoA bytes."""
+        from cabanapic_gb300 import layout as L
+        R = deck.R
+        n = deck.num_particles
+        buf = np.empty(L.particle_list_bytes(n, R, deck.vl), np.uint8)
+        getattr(self.lib, f"orc_thermal_particles_{self._suf(R)}")(
+            _ptr(buf), n, deck.vl, deck.nppc, deck.nx, deck.ny, float(deck.extra.get("uth", 0.05)),
+            float(deck.derived()["we"]), int(deck.extra.get("seed", 2024)) & (2 ** 64 - 1))
+        return buf
 
     def num_threads(self) -> int:
         return self.lib.orc_num_threads()

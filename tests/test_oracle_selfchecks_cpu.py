@@ -76,3 +76,18 @@ def test_omp_push_matches_serial_push(orc):
     assert np.array_equal(serial, omp)
     bound = reorder_bound(acc_abs, acc_cnt, np.finfo(np.float32).eps)
     assert np.all(np.abs(acc_o.astype(np.float64) - acc_s) <= bound + 1e-30)
+
+
+@pytest.mark.parametrize("precision", [4, 8])
+def test_oracle_thermal_loader_matches_host_restatement(orc, precision):
+    """The oracle's OpenMP thermal loader (the CPU baseline's input at full
+    size) gives the host restatement's particles: offsets, weights and cells
+    bit for bit, momenta within one rounding of the libm calls."""
+    d = decks.thermal(n=10, ppc=7, precision=precision, seed=99)
+    want = decks.thermal_particles(d)
+    got = L.unpack_particles(orc.thermal_particles(d), d.num_particles, d.R, d.vl)
+    for k in ("x", "y", "z", "w", "cell"):
+        assert np.array_equal(got[k], want[k]), k
+    eps = np.finfo(d.R).eps
+    for k in ("ux", "uy", "uz"):
+        assert np.all(np.abs(got[k] - want[k]) <= 2 * eps * np.abs(want[k])), k
