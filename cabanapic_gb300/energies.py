@@ -28,11 +28,19 @@ def _fmt(v: float) -> str:
     return s
 
 
-def energy_line(step: int, time: float, e: float, b: float) -> str:
+def energy_line(step: int, time: float, e: float, b: float = None) -> str:
+    """The energies.txt line; b=None gives the ES solvers' `step time E`
+    line (fields.h:751-759 writes B only for the EM solver)."""
+    if b is None:
+        return f"{step} {_fmt(time)} {_fmt(e)}"
     return f"{step} {_fmt(time)} {_fmt(e)} {_fmt(b)}"
 
 
-def stdout_line(step: int, time: float, e: float, b: float) -> str:
+def stdout_line(step: int, time: float, e: float, b: float = None) -> str:
+    """printf("%d %f %e %e") of the EM solver, printf("%d %f %e") when b is
+    None (the ES solvers)."""
+    if b is None:
+        return f"{step} {time:f} {e:e}"
     return f"{step} {time:f} {e:e} {b:e}"
 
 

@@ -266,13 +266,19 @@ class ESFieldSolver1D:
         return float(out[0].item())
 
 
-def dump_energies(field_solver: EMFieldSolver, fields: FieldArray, step, time, px, py, pz, nx, ny,
+def dump_energies(field_solver, fields: FieldArray, step, time, px, py, pz, nx, ny,
                   nz, ng, path: str = "energies.txt", echo: bool = True) -> tuple:
     """dump_energies (src/fields.h:722-763): appends the `step time E B` line
     to `path` in std::ostream format (truncating the file at step 0) and, as
     the reference does, prints the printf("%d %f %e %e") line to stdout
-    (echo=False leaves stdout alone).  Returns (E, B)."""
-    e, b = field_solver.energies_async(fields, nx, ny, nz, ng).cpu().tolist()
+    (echo=False leaves stdout alone).  Returns (E, B).  With an ES solver
+    (ESFieldSolver1D, the reference's ES_FIELD_SOLVER build) there is no B:
+    the line is `step time E`, the stdout line printf("%d %f %e"), and B is
+    returned as None."""
+    if isinstance(field_solver, ESFieldSolver1D):
+        e, b = field_solver.e_energy(fields, px, py, pz, nx, ny, nz, ng), None
+    else:
+        e, b = field_solver.energies_async(fields, nx, ny, nz, ng).cpu().tolist()
     mode = "w" if step == 0 else "a"
     with open(path, mode) as fh:
         fh.write(_energies.energy_line(step, time, e, b) + "\n")

@@ -25,6 +25,10 @@ int main(int argc, char** argv) {
     std::cout << step << " " << t << " " << e << " " << b << std::endl;
     std::printf("%d %f %e %e\n", step, t, e, b);
     std::fflush(stdout);
+    // the ES_FIELD_SOLVER build: no B token
+    std::cout << step << " " << t << " " << e << std::endl;
+    std::printf("%d %f %e\n", step, t, e);
+    std::fflush(stdout);
   }
   return 0;
 }
@@ -45,7 +49,7 @@ def cpp_format(tmp_path_factory):
         inp = "".join(f"{s} {t!r} {e!r} {b!r}\n" for s, t, e, b in rows)
         out = subprocess.run([str(exe)], input=inp, capture_output=True, text=True, check=True).stdout
         lines = out.splitlines()
-        return lines[0::2], lines[1::2]
+        return lines[0::4], lines[1::4], lines[2::4], lines[3::4]
 
     return run
 
@@ -63,11 +67,24 @@ def _rows():
 
 def test_ostream_and_printf_lines_match_the_c_libraries(cpp_format):
     rows = _rows()
-    ostream, printf = cpp_format(rows)
-    assert len(ostream) == len(rows) == len(printf)
-    for (s, t, e, b), lo, lp in zip(rows, ostream, printf):
+    ostream, printf, ostream_es, printf_es = cpp_format(rows)
+    assert len(ostream) == len(rows) == len(printf) == len(ostream_es) == len(printf_es)
+    for (s, t, e, b), lo, lp, leo, lep in zip(rows, ostream, printf, ostream_es, printf_es):
         assert E.energy_line(s, t, e, b) == lo
         assert E.stdout_line(s, t, e, b) == lp
+        assert E.energy_line(s, t, e) == leo
+        assert E.stdout_line(s, t, e) == lep
+
+
+def test_oracle_formatter_agrees_with_the_product_formatter(cpp_format):
+    """The oracle keeps its own restatement of the energies.txt line (test
+    infrastructure does not import the product's formatter); both must give
+    the same text, here on the gold values and on the C-checked rows."""
+    from oracle import energy_rule
+    g = np.loadtxt(gold_path("double"))
+    rows = [(int(r[0]), r[1], r[2], r[3]) for r in g] + _rows()
+    for s, t, e, b in rows:
+        assert energy_rule.format_energy_line(s, t, e, b) == E.energy_line(s, t, e, b)
 
 
 @pytest.mark.parametrize("kind", ["float", "double"])
@@ -120,6 +137,32 @@ def test_pic_dump_energies_writes_the_file_and_echoes_the_stdout_line(tmp_path, 
     pic.dump_energies(s, None, 0, 0.0, 0, 0, 0, 4, 4, 4, 1, path=str(path), echo=False)
     assert path.read_text().splitlines() == [E.energy_line(0, 0.0, *vals[0])]
     assert capsys.readouterr().out == ""
+
+
+def test_pic_dump_energies_with_an_es_solver(tmp_path, capsys):
+    """With an ES solver (the reference's ES_FIELD_SOLVER build) dump_energies
+    writes and prints `step time E` only (src/fields.h:751-759)."""
+    pytest.importorskip("torch")
+    from cabanapic_gb300 import pic
+
+    vals = [4.25e-3, 3.5e-3]
+
+    class Solver(pic.ESFieldSolver1D):
+        step = 0
+
+        def e_energy(self, fields, px, py, pz, nx, ny, nz, ng, *, stream=None):
+            return vals[self.step]
+
+    path = tmp_path / "energies.txt"
+    s = Solver()
+    dt = 0.0195487
+    for k in range(2):
+        s.step = k
+        e, b = pic.dump_energies(s, None, k, k * dt, 0, 0, 0, 32, 1, 1, 1, path=str(path))
+        assert (e, b) == (vals[k], None)
+    assert path.read_text().splitlines() == [E.energy_line(k, k * dt, vals[k]) for k in range(2)]
+    assert capsys.readouterr().out.splitlines() == [E.stdout_line(k, k * dt, vals[k]) for k in range(2)]
+    assert all(len(l.split(" ")) == 3 for l in path.read_text().splitlines())
 
 
 _CPP_PAIRS = r"""
