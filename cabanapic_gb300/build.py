@@ -68,11 +68,18 @@ def _newest_input() -> float:
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
     """Compiles libcpic.so (and the minipic driver); returns the library path."""
     os.makedirs(OUT, exist_ok=True)
-    if (not force and os.path.exists(LIB) and os.path.exists(MINIPIC) and os.path.exists(MINIPIC_F64)
-            and os.path.getmtime(LIB) >= _newest_input()):
+    # tuning macros of the push kernels (tile shapes), e.g.
+    # CPIC_NVCC_FLAGS="-DCPIC_TILE_CHUNKS=5 -DCPIC_TILE_WXMAX=44"; a change of
+    # flags rebuilds
+    stamp = os.path.join(OUT, "nvcc_flags.txt")
+    flags_now = os.environ.get("CPIC_NVCC_FLAGS", "")
+    flags_then = open(stamp).read() if os.path.exists(stamp) else ""
+    if (not force and flags_now == flags_then and os.path.exists(LIB) and os.path.exists(MINIPIC)
+            and os.path.exists(MINIPIC_F64) and os.path.getmtime(LIB) >= _newest_input()):
         return LIB
     nvcc = _nvcc()
     extra = ["-Xptxas", "-v"] if ptxas_info else []
+    extra += flags_now.split()
 
     def compile_one(src):
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
@@ -104,6 +111,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     with ThreadPoolExecutor(max_workers=2) as ex:
         list(ex.map(link_driver, [(MINIPIC, []), (MINIPIC_F64, ["-DREAL_TYPE=double"])]))
+    with open(stamp, "w") as fh:
+        fh.write(flags_now)
     return LIB
 
 

@@ -825,8 +825,14 @@ struct TileShape {
 // the per-tile staging and measured faster than windows that cover the
 // whole tile (4 chunks and 36 voxels: 2.55 ms, 7 and 44: 2.47 ms at 128^3 x
 // 64 ppc; 48-voxel windows cross the carveout and cost 5%).
+#ifndef CPIC_TILE_CHUNKS
+#define CPIC_TILE_CHUNKS 7  // chunks per consumer warp and tile
+#endif
+#ifndef CPIC_TILE_WXMAX
+#define CPIC_TILE_WXMAX 44  // longest window segment (voxels)
+#endif
 inline TileShape tile_shape(const GridDev& g) {
-  TileShape ts{7, 44};
+  TileShape ts{CPIC_TILE_CHUNKS, CPIC_TILE_WXMAX};
   if (ts.wxmax > g.sx) ts.wxmax = g.sx;  // segments of one window must not overlap
   if (ts.wxmax < 3) ts.wxmax = 3;
   return ts;

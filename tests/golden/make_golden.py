@@ -6,7 +6,8 @@ the reference tree: 6000 rows of `step time E B`).  The machines that run the
 GPU tests do not have the reference tree, so the fixtures are committed; this script regenerates
 them from a checkout of the reference.
 
-usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+usage: python tests/golden/make_golden.py REFERENCE_ROOT
+   or: CABANAPIC_REFERENCE=REFERENCE_ROOT python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -26,4 +27,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CABANAPIC_REFERENCE")
+    if not root:
+        sys.exit(__doc__)
+    main(root)
