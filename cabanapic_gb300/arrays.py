@@ -142,12 +142,20 @@ class FieldArray(_CellArray):
 
 
 class AccumulatorArray:
-    """accumulator_array_t: View<real_t*[3][4]> in LayoutRight."""
+    """accumulator_array_t: View<real_t*[3][4]> in LayoutRight ([cell][comp][q],
+    the reference's host build), or with layout="left" in Kokkos' LayoutLeft
+    (the Kokkos-Cuda default: value (comp, q) of cell c at c + num_cells (comp
+    + 3 q), stored here as a [q][comp][cell] tensor).  get() and set() take
+    (num_cells, 3, 4) values in either layout."""
 
-    def __init__(self, num_cells: int, real=np.float32, device=None):
+    def __init__(self, num_cells: int, real=np.float32, device=None, layout: str = "right"):
+        if layout not in ("right", "left"):
+            raise ValueError("layout is 'right' or 'left'")
         self.num_cells = int(num_cells)
         self.real = np.dtype(real)
-        self.buf = torch.zeros((self.num_cells, 3, 4), dtype=_torch_real(self.real), device=_dev(device))
+        self.layout = layout
+        shape = (self.num_cells, 3, 4) if layout == "right" else (4, 3, self.num_cells)
+        self.buf = torch.zeros(shape, dtype=_torch_real(self.real), device=_dev(device))
 
     @property
     def precision(self) -> int:
@@ -161,7 +169,11 @@ class AccumulatorArray:
         return self.num_cells
 
     def get(self) -> np.ndarray:
-        return self.buf.cpu().numpy()
+        a = self.buf.cpu().numpy()
+        return a if self.layout == "right" else np.ascontiguousarray(a.transpose(2, 1, 0))
 
     def set(self, vals: np.ndarray) -> None:
-        self.buf.copy_(torch.from_numpy(np.asarray(vals, self.real).reshape(self.num_cells, 3, 4)))
+        v = np.asarray(vals, self.real).reshape(self.num_cells, 3, 4)
+        if self.layout == "left":
+            v = np.ascontiguousarray(v.transpose(2, 1, 0))
+        self.buf.copy_(torch.from_numpy(v))

@@ -11,7 +11,9 @@ multiply-adds.
 
 The C++ example driver (csrc/minipic.cpp: the reference's time loop written
 against the C++ push() interface in include/cpic/cabana.hpp) is linked into
-cabanapic_gb300/_build/minipic (real_t = float) and minipic_f64 (real_t = double).
+cabanapic_gb300/_build/minipic (real_t = float), minipic_f64 (real_t = double) and
+minipic_f64_left (real_t = double, the accumulator in Kokkos' LayoutLeft as in a
+Kokkos-Cuda build).
 """
 from __future__ import annotations
 
@@ -29,6 +31,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcpic.so")
 MINIPIC = os.path.join(OUT, "minipic")
 MINIPIC_F64 = os.path.join(OUT, "minipic_f64")
+MINIPIC_F64_LEFT = os.path.join(OUT, "minipic_f64_left")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
@@ -75,7 +78,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     flags_now = os.environ.get("CPIC_NVCC_FLAGS", "")
     flags_then = open(stamp).read() if os.path.exists(stamp) else ""
     if (not force and flags_now == flags_then and os.path.exists(LIB) and os.path.exists(MINIPIC)
-            and os.path.exists(MINIPIC_F64) and os.path.getmtime(LIB) >= _newest_input()):
+            and os.path.exists(MINIPIC_F64) and os.path.exists(MINIPIC_F64_LEFT)
+            and os.path.getmtime(LIB) >= _newest_input()):
         return LIB
     nvcc = _nvcc()
     extra = ["-Xptxas", "-v"] if ptxas_info else []
@@ -109,8 +113,9 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
               "-Xlinker", "-rpath=$ORIGIN"])
         os.replace(exe + ".tmp", exe)
 
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        list(ex.map(link_driver, [(MINIPIC, []), (MINIPIC_F64, ["-DREAL_TYPE=double"])]))
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        list(ex.map(link_driver, [(MINIPIC, []), (MINIPIC_F64, ["-DREAL_TYPE=double"]),
+                                  (MINIPIC_F64_LEFT, ["-DREAL_TYPE=double", "-DCPIC_ACCUMULATOR_LAYOUT_LEFT"])]))
     with open(stamp, "w") as fh:
         fh.write(flags_now)
     return LIB

@@ -30,6 +30,7 @@ CPIC_PUSH_TRUE_SQRT = 1
 CPIC_PUSH_EXACT = 2
 CPIC_PUSH_STREAMING = 4
 CPIC_PUSH_ACC_F64 = 8
+CPIC_PUSH_ACC_LAYOUT_LEFT = 16
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -111,6 +112,7 @@ _SIGS = {
     "cpic_sort_into_scratch_bytes": (_sz, [_i64, _i64, _i32, _i32]),
     "cpic_sort_particles_into": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp, _sz, _vp]),
     "cpic_unload_accumulator_f64": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64, _i32, _vp]),
+    "cpic_unload_accumulator_left": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64, _i32, _vp]),
     "cpic_thermal_particles": (_i32, [_vp, _i64, _i32, C.POINTER(CpicGrid), _f64, _f64, C.c_uint64, _i32,
                                       _i32, _vp]),
     "cpic_selftest_bounded_wait": (_i32, [_i64, _vp, _vp]),

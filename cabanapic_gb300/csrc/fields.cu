@@ -65,14 +65,19 @@ load_interpolator_kernel(const R* __restrict__ F, R* __restrict__ I, const GridD
 
 // ------------------------------------------------------------ accumulator
 // unload_accumulator_array (accumulator.cpp:71-110): cells [1, n+1] per axis.
-template <class R, class Acc = R>
+// LEFT: the accumulator in Kokkos' LayoutLeft (value k = 4 comp + q of cell c
+// at c + num_cells (comp + 3 q)); the sums are the same, in the same order.
+template <class R, class Acc = R, bool LEFT = false>
 __global__ void __launch_bounds__(kThreads)
 unload_kernel(R* __restrict__ F, const Acc* __restrict__ A, const GridDev g, Acc cx, Acc cy, Acc cz,
               int begin, int end) {
   constexpr int K = 2;
   const int c0 = lane_cell0<K, kThreads>(begin);
   const int oy = g.sx, oz = g.sx * g.sy;
-  auto a = [&](int c, int k) { return __ldg(A + (size_t)c * 12 + k); };
+  auto a = [&](int c, int k) {
+    if constexpr (LEFT) return __ldg(A + (size_t)c + (size_t)g.num_cells * ((k >> 2) + 3 * (k & 3)));
+    else return __ldg(A + (size_t)c * 12 + k);
+  };
   Acc v[K][12];
   bool ok[K];
 #pragma unroll
@@ -405,7 +410,7 @@ static int typed_load_interp(const void* f, void* i, const GridDev& g, cudaStrea
   return launch_status();
 }
 
-template <class R, class Acc = R>
+template <class R, class Acc = R, bool LEFT = false>
 static int typed_unload(void* f, const void* a, const GridDev& g, double dx, double dy, double dz,
                         double dt, cudaStream_t s) {
   const R rdx = (R)dx, rdy = (R)dy, rdz = (R)dz, rdt = (R)dt;
@@ -414,7 +419,7 @@ static int typed_unload(void* f, const void* a, const GridDev& g, double dx, dou
   const R cy = (R)(0.25 / (double)(R)(rdz * rdx * rdt));
   const R cz = (R)(0.25 / (double)(R)(rdx * rdy * rdt));
   const CellRange r = cell_range<2, kThreads>(g, g.nx + 1, g.ny + 1, g.nz + 1);
-  unload_kernel<R, Acc><<<r.blocks, kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const Acc*>(a), g,
+  unload_kernel<R, Acc, LEFT><<<r.blocks, kThreads, 0, s>>>(static_cast<R*>(f), static_cast<const Acc*>(a), g,
                                                       (Acc)cx, (Acc)cy, (Acc)cz, r.begin, r.end);
   return launch_status();
 }
@@ -524,6 +529,19 @@ extern "C" int cpic_unload_accumulator(void* fields, const void* accumulators, c
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   return precision == CPIC_FLOAT ? typed_unload<float>(fields, accumulators, g, dx, dy, dz, dt, s)
                                  : typed_unload<double>(fields, accumulators, g, dx, dy, dz, dt, s);
+}
+
+extern "C" int cpic_unload_accumulator_left(void* fields, const void* accumulators, const cpic_grid* grid,
+                                            double dx, double dy, double dz, double dt, int32_t precision,
+                                            cpic_stream_t stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  CPIC_CHECK_PREC(precision);
+  if (!fields || !accumulators) return CPIC_EINVAL;
+  const GridDev g = make_grid(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return precision == CPIC_FLOAT ? typed_unload<float, float, true>(fields, accumulators, g, dx, dy, dz, dt, s)
+                                 : typed_unload<double, double, true>(fields, accumulators, g, dx, dy, dz, dt, s);
 }
 
 extern "C" int cpic_unload_accumulator_f64(void* fields, const double* accumulators, const cpic_grid* grid,

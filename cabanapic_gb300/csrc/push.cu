@@ -26,8 +26,11 @@ int check_push_args(int64_t num_particles, const cpic_grid* grid, const cpic_pus
   if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
   if (prm->precision != CPIC_FLOAT && prm->precision != CPIC_DOUBLE) return CPIC_EINVAL;
   if (prm->particle_vl != 16 && prm->particle_vl != 32) return CPIC_EINVAL;
-  if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT | CPIC_PUSH_STREAMING | CPIC_PUSH_ACC_F64))
+  if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT | CPIC_PUSH_STREAMING | CPIC_PUSH_ACC_F64 |
+                     CPIC_PUSH_ACC_LAYOUT_LEFT))
     return CPIC_EINVAL;
+  // LayoutLeft with double rows for FP32 particles has no unload entry point
+  if ((prm->flags & CPIC_PUSH_ACC_LAYOUT_LEFT) && (prm->flags & CPIC_PUSH_ACC_F64)) return CPIC_EINVAL;
   return CPIC_OK;
 }
 }  // namespace

@@ -62,10 +62,23 @@
 
 namespace cpic {
 
+// Where value vi = 4 comp + q of a cell's accumulator lives: LayoutRight rows
+// [cell][3][4] (12 contiguous values, the reference's host build), or the
+// Kokkos-Cuda default LayoutLeft [q][comp][cell] (value (comp, q) of cell c
+// at c + n (comp + 3 q), n = num_cells: src/types.h:120 under a Cuda build).
+struct AccMap {
+  int left;  // 0: LayoutRight
+  int n;     // the accumulator's first extent (num_cells)
+  __device__ __forceinline__ size_t at(int cell, int vi) const {
+    return left ? (size_t)cell + (size_t)n * (size_t)((vi >> 2) + 3 * (vi & 3)) : (size_t)cell * 12 + vi;
+  }
+};
+
 template <class R>
 struct PushArgs {
   R qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp;
   GridDev g;
+  AccMap acc;
 };
 
 // Cell window of one tile: segments [c0 + off_s, c0 + off_s + wx) with
@@ -184,10 +197,22 @@ __device__ __forceinline__ void red_add12(Acc* __restrict__ a, const R v[12]) {
   red_add4(a + 8, (Acc)v[8], (Acc)v[9], (Acc)v[10], (Acc)v[11]);
 }
 
+// Adds 12 deposits to `cell`'s accumulator values in either layout (LayoutLeft:
+// 12 scalar reductions, n apart).
+template <class R, class Acc>
+__device__ __forceinline__ void red_add12(Acc* __restrict__ acc, const AccMap& m, int cell, const R v[12]) {
+  if (m.left) {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) red_add(acc + m.at(cell, k), (Acc)v[k]);
+  } else {
+    red_add12(acc + (size_t)cell * 12, v);
+  }
+}
+
 // Deposit of the in-cell particles of one warp into accumulator_array.  `dep`
 // lanes add v[0..11] to accumulator row `cell`; `vi` is value_of_lane(lane).
 template <class R, class Acc>
-__device__ __forceinline__ void warp_deposit(Acc* __restrict__ acc, int cell, bool dep,
+__device__ __forceinline__ void warp_deposit(Acc* __restrict__ acc, const AccMap& am, int cell, bool dep,
                                              const R v[12], int lane, int vi) {
   const unsigned dm = __ballot_sync(kFull, dep);
   if (dm == 0u) return;
@@ -197,7 +222,7 @@ __device__ __forceinline__ void warp_deposit(Acc* __restrict__ acc, int cell, bo
 #pragma unroll
     for (int k = 0; k < 12; ++k) w[k] = dep ? v[k] : R(0);
     const R tot = reduce_scatter12<R>(w, lane);
-    if (vi >= 0) red_add(acc + (size_t)cell0 * 12 + vi, (Acc)tot);
+    if (vi >= 0) red_add(acc + am.at(cell0, vi), (Acc)tot);
     return;
   }
   const int key = dep ? cell : -1 - lane;
@@ -214,9 +239,9 @@ __device__ __forceinline__ void warp_deposit(Acc* __restrict__ acc, int cell, bo
     for (int k = 0; k < 12; ++k) w[k] = in_major ? v[k] : R(0);
     const R tot = reduce_scatter12<R>(w, lane);
     const int major_cell = __shfl_sync(kFull, cell, leader);
-    if (vi >= 0) red_add(acc + (size_t)major_cell * 12 + vi, (Acc)tot);
+    if (vi >= 0) red_add(acc + am.at(major_cell, vi), (Acc)tot);
   }
-  if (dep && !in_major) red_add12(acc + (size_t)cell * 12, v);
+  if (dep && !in_major) red_add12(acc, am, cell, v);
 }
 
 // Twice the fractional distance to a face, (dir - p) / s (move_p.h:115-117).
@@ -237,7 +262,7 @@ __device__ __forceinline__ R face_fraction(R dir, R p, R s) {
 template <class R, int VL, bool FAST, class Acc>
 __device__ __forceinline__ void move_one(unsigned char* __restrict__ part, R px, R py, R pz, R dx,
                                       R dy, R dz, R q, int cell, int pidx, Acc* __restrict__ acc,
-                                      const GridDev g, int* __restrict__ status) {
+                                      const GridDev g, const AccMap& am, int* __restrict__ status) {
   using L = PLayout<R, VL>;
   if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) atomicOr(status, CPIC_STATUS_NONFINITE);
   bool done = false;
@@ -267,7 +292,7 @@ __device__ __forceinline__ void move_one(unsigned char* __restrict__ part, R px,
     const R corr = (R)((double)(q * sx * sy * sz) * (1. / 3.));
     R v[12];
     currents12<R>(q, sx, sy, sz, mx, my, mz, corr, v);
-    red_add12(acc + (size_t)cell * 12, v);
+    red_add12(acc, am, cell, v);
     dx -= sx; dy -= sy; dz -= sz;
     px += sx + sx; py += sy + sy; pz += sz + sz;
     if (axis == 3) { done = true; break; }
@@ -489,7 +514,7 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
   R v[12];
   const R corr = q * ux * uy * uz * one_third;
   currents12<R>(q, ux, uy, uz, mx, my, mz, corr, v);
-  warp_deposit<R, Acc>(acc, cell, inb, v, lc.lane, lc.vi);
+  warp_deposit<R, Acc>(acc, a.acc, cell, inb, v, lc.lane, lc.vi);
 
   // compact the cell-crossing particles into the warp queue
   const bool cross = valid && !inb;
@@ -510,7 +535,7 @@ __device__ __forceinline__ void push_chunk(unsigned char* __restrict__ part, int
       const int cc = Q.cell[s], ii = Q.idx[s];
       __syncwarp();
       qn -= 32;
-      move_one<R, VL, FAST, Acc>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, status);
+      move_one<R, VL, FAST, Acc>(part, ex0, ey0, ez0, ddx, ddy, ddz, qq, cc, ii, acc, a.g, a.acc, status);
     }
   }
 }
@@ -535,7 +560,7 @@ __device__ __forceinline__ void drain_queue(unsigned char* __restrict__ part, Mo
   __syncwarp();
   if (lane < qn)
     move_one<R, VL, FAST, Acc>(part, Q.px[lane], Q.py[lane], Q.pz[lane], Q.dx[lane], Q.dy[lane], Q.dz[lane],
-                    Q.q[lane], Q.cell[lane], Q.idx[lane], acc, a.g, status);
+                    Q.q[lane], Q.cell[lane], Q.idx[lane], acc, a.g, a.acc, status);
 }
 
 // ------------------------------------------------------------ streaming kernel
@@ -896,9 +921,10 @@ int push_dispatch(void* particles, int n, const void* interp, void* acc, const c
   const GridDev gd = make_grid(g);
   // the window arithmetic keeps 3 * sx * sy and cell + sx * sy + sx in int range
   const bool tiled = !(prm->flags & CPIC_PUSH_STREAMING) && gd.num_cells <= (1 << 30);
+  const AccMap am{(prm->flags & CPIC_PUSH_ACC_LAYOUT_LEFT) ? 1 : 0, gd.num_cells};
   if (prm->precision == CPIC_FLOAT) {
     PushArgs<float> a{(float)prm->qdt_2mc, (float)prm->cdt_dx, (float)prm->cdt_dy,
-                      (float)prm->cdt_dz, (float)prm->qsp, gd};
+                      (float)prm->cdt_dz, (float)prm->qsp, gd, am};
     if (prm->flags & CPIC_PUSH_ACC_F64)  // FP32 particles, FP64 accumulator rows
       return prm->particle_vl == 32
                  ? launch_any<float, 32, true, FAST, double>(tiled, particles, n, interp, acc, a, status, s)
@@ -906,7 +932,7 @@ int push_dispatch(void* particles, int n, const void* interp, void* acc, const c
     return prm->particle_vl == 32 ? launch_any<float, 32, true, FAST>(tiled, particles, n, interp, acc, a, status, s)
                                   : launch_any<float, 16, true, FAST>(tiled, particles, n, interp, acc, a, status, s);
   }
-  PushArgs<double> a{prm->qdt_2mc, prm->cdt_dx, prm->cdt_dy, prm->cdt_dz, prm->qsp, gd};
+  PushArgs<double> a{prm->qdt_2mc, prm->cdt_dx, prm->cdt_dy, prm->cdt_dz, prm->qsp, gd, am};
   if (prm->particle_vl == 32)
     return literal ? launch_any<double, 32, true, FAST>(tiled, particles, n, interp, acc, a, status, s)
                    : launch_any<double, 32, false, FAST>(tiled, particles, n, interp, acc, a, status, s);
@@ -922,9 +948,10 @@ int push_into_dispatch(const void* src, void* dst, int n, const void* interp, vo
   const bool literal = !(prm->flags & CPIC_PUSH_TRUE_SQRT);
   const GridDev gd = make_grid(g);
   if (gd.num_cells > (1 << 30)) return CPIC_EUNSUPPORTED;
+  const AccMap am{(prm->flags & CPIC_PUSH_ACC_LAYOUT_LEFT) ? 1 : 0, gd.num_cells};
   if (prm->precision == CPIC_FLOAT) {
     PushArgs<float> a{(float)prm->qdt_2mc, (float)prm->cdt_dx, (float)prm->cdt_dy,
-                      (float)prm->cdt_dz, (float)prm->qsp, gd};
+                      (float)prm->cdt_dz, (float)prm->qsp, gd, am};
     if (prm->flags & CPIC_PUSH_ACC_F64)
       return prm->particle_vl == 32
                  ? launch_push_tiled<float, 32, true, FAST, double, true>(dst, n, interp, acc, a, status, s, src)
@@ -933,7 +960,7 @@ int push_into_dispatch(const void* src, void* dst, int n, const void* interp, vo
                ? launch_push_tiled<float, 32, true, FAST, float, true>(dst, n, interp, acc, a, status, s, src)
                : launch_push_tiled<float, 16, true, FAST, float, true>(dst, n, interp, acc, a, status, s, src);
   }
-  PushArgs<double> a{prm->qdt_2mc, prm->cdt_dx, prm->cdt_dy, prm->cdt_dz, prm->qsp, gd};
+  PushArgs<double> a{prm->qdt_2mc, prm->cdt_dx, prm->cdt_dy, prm->cdt_dz, prm->qsp, gd, am};
   if (prm->particle_vl == 32)
     return literal ? launch_push_tiled<double, 32, true, FAST, double, true>(dst, n, interp, acc, a, status, s, src)
                    : launch_push_tiled<double, 32, false, FAST, double, true>(dst, n, interp, acc, a, status, s, src);

@@ -106,8 +106,10 @@ def _push_args(fn, particles, f0, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, a0, nx, 
                boundary, true_sqrt, exact, tiles):
     # an FP64 accumulator with FP32 particles: the compensated per-cell current sum
     acc_f64 = particles.precision == capi.CPIC_FLOAT and a0.precision == capi.CPIC_DOUBLE
+    left = getattr(a0, "layout", "right") == "left"
     flags = ((capi.CPIC_PUSH_TRUE_SQRT if true_sqrt else 0) | (capi.CPIC_PUSH_EXACT if exact else 0)
-             | (0 if tiles else capi.CPIC_PUSH_STREAMING) | (capi.CPIC_PUSH_ACC_F64 if acc_f64 else 0))
+             | (0 if tiles else capi.CPIC_PUSH_STREAMING) | (capi.CPIC_PUSH_ACC_F64 if acc_f64 else 0)
+             | (capi.CPIC_PUSH_ACC_LAYOUT_LEFT if left else 0))
     prm = capi.CpicPushParams(float(qdt_2mc), float(cdt_dx), float(cdt_dy), float(cdt_dz),
                               float(qsp), particles.precision, particles.vl, flags, 0)
     if f0.precision != particles.precision or (a0.precision != particles.precision and not acc_f64):
@@ -168,10 +170,14 @@ def unload_accumulator_array(fields: FieldArray, accumulators: AccumulatorArray,
                              dx, dy, dz, dt, *, boundary=Boundary.Periodic, stream=None) -> None:
     """unload_accumulator_array (src/accumulator.cpp:45-122).  An FP64
     accumulator with FP32 fields (the compensated current sum of an FP32 push)
-    is unloaded in double and rounded once."""
-    fn = ("cpic_unload_accumulator_f64"
-          if accumulators.precision == capi.CPIC_DOUBLE and fields.precision == capi.CPIC_FLOAT
-          else "cpic_unload_accumulator")
+    is unloaded in double and rounded once; a LayoutLeft accumulator
+    (AccumulatorArray(layout="left")) through cpic_unload_accumulator_left."""
+    if getattr(accumulators, "layout", "right") == "left":
+        fn = "cpic_unload_accumulator_left"
+    elif accumulators.precision == capi.CPIC_DOUBLE and fields.precision == capi.CPIC_FLOAT:
+        fn = "cpic_unload_accumulator_f64"
+    else:
+        fn = "cpic_unload_accumulator"
     capi.load().call(fn, fields.ptr, accumulators.ptr,
                      C.byref(_grid(nx, ny, nz, ng, boundary)), float(dx), float(dy), float(dz),
                      float(dt), fields.precision, _stream(stream))

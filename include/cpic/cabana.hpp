@@ -114,9 +114,17 @@ class cell_aosoa_t {
 typedef cell_aosoa_t<CPIC_INTERP_MEMBERS> interpolator_array_t;
 typedef cell_aosoa_t<CPIC_FIELD_MEMBERS> field_array_t;
 
-// accumulator_array_t: Kokkos::View<real_t*[3][4]> (LayoutRight)
+// accumulator_array_t: Kokkos::View<real_t*[3][4]>, LayoutRight (the
+// reference's host build) unless CPIC_ACCUMULATOR_LAYOUT_LEFT is defined: then
+// Kokkos' LayoutLeft, the layout the same View has in a Kokkos-Cuda build
+// (src/types.h:120); push and unload_accumulator_array follow.
 class accumulator_array_t {
  public:
+#ifdef CPIC_ACCUMULATOR_LAYOUT_LEFT
+  static constexpr bool layout_left = true;
+#else
+  static constexpr bool layout_left = false;
+#endif
   accumulator_array_t(const char* /*label*/, size_t num_cells)
       : n_(num_cells), mem_(num_cells * CPIC_ACC_VALUES * sizeof(real_t)) {}
   size_t extent(int) const { return n_; }
@@ -192,7 +200,7 @@ void push(particle_list_t& particles, interpolator_array_t& f0, real_t qdt_2mc, 
   cpic_push_params prm;
   prm.qdt_2mc = qdt_2mc; prm.cdt_dx = cdt_dx; prm.cdt_dy = cdt_dy; prm.cdt_dz = cdt_dz;
   prm.qsp = qsp; prm.precision = cpic::kReal; prm.particle_vl = particle_list_t::vector_length;
-  prm.flags = 0; prm.reserved = 0;
+  prm.flags = accumulator_array_t::layout_left ? CPIC_PUSH_ACC_LAYOUT_LEFT : 0; prm.reserved = 0;
   cpic::check(cpic_push(particles.data(), (int64_t)particles.size(), f0.data(), cpic::acc_ptr(a0),
                         &grid, &prm, cpic::status_word(), cpic::current_stream()),
               "push");
@@ -227,8 +235,8 @@ inline void unload_accumulator_array(field_array_t& fields, accumulator_array_t&
                                      size_t nx, size_t ny, size_t nz, size_t ng, real_t dx,
                                      real_t dy, real_t dz, real_t dt) {
   cpic_grid g = cpic::make_grid(nx, ny, nz, ng, cpic::field_boundary());
-  cpic::check(cpic_unload_accumulator(fields.data(), accumulators.data(), &g, dx, dy, dz, dt,
-                                      cpic::kReal, cpic::current_stream()),
+  auto unload = accumulator_array_t::layout_left ? cpic_unload_accumulator_left : cpic_unload_accumulator;
+  cpic::check(unload(fields.data(), accumulators.data(), &g, dx, dy, dz, dt, cpic::kReal, cpic::current_stream()),
               "unload_accumulator_array");
 }
 

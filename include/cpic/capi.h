@@ -72,6 +72,14 @@ typedef struct CUstream_st* cpic_stream_t;
                                   particles per cell) runs in double, so its error no longer
                                   grows with k.  Unload with cpic_unload_accumulator_f64. */
 
+#define CPIC_PUSH_ACC_LAYOUT_LEFT 16 /* `accumulators` in Kokkos' LayoutLeft, the default
+                                  layout of accumulator_array_t = View<real_t*[3][4]> in a
+                                  Kokkos-Cuda build (src/types.h:120): value (comp, q) of cell c
+                                  at c + num_cells * (comp + 3 q), num_cells the grid's ghosted
+                                  cell count (the extent example/example.cpp:137 allocates).
+                                  Unload with cpic_unload_accumulator_left.  Not with
+                                  CPIC_PUSH_ACC_F64. */
+
 /* Grid of the run: interior cells nx*ny*nz plus num_ghosts ghost layers;
  * boundary is the deck's BOUNDARY_TYPE, which the reference's field code reads
  * from the global deck (src/fields.h:20,112). */
@@ -144,6 +152,14 @@ int cpic_clear_accumulator(void* accumulators, int64_t num_cells, int32_t precis
 int cpic_unload_accumulator(void* fields, const void* accumulators, const cpic_grid* grid,
                             double dx, double dy, double dz, double dt, int32_t precision,
                             cpic_stream_t stream);
+
+/* Replaces: unload_accumulator_array (src/accumulator.cpp:45-122) for an
+ * accumulator in Kokkos' LayoutLeft, the Kokkos-Cuda default of
+ * src/types.h:120 (see CPIC_PUSH_ACC_LAYOUT_LEFT): the same sums in the same
+ * order as cpic_unload_accumulator, so the same jf bits. */
+int cpic_unload_accumulator_left(void* fields, const void* accumulators, const cpic_grid* grid,
+                                 double dx, double dy, double dz, double dt, int32_t precision,
+                                 cpic_stream_t stream);
 
 /* unload_accumulator_array from the double accumulator rows of a push with
  * CPIC_PUSH_ACC_F64: the four-term sums and the scaling run in double, jf is

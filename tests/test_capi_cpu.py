@@ -66,7 +66,10 @@ def test_push_argument_validation(lib):
     assert push(dummy, 10, dummy, dummy, C.byref(g), None, C.byref(status), None) == capi.CPIC_EINVAL
     assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(precision=2)), C.byref(status), None) == capi.CPIC_EINVAL
     assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(particle_vl=8)), C.byref(status), None) == capi.CPIC_EINVAL
-    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(flags=16)), C.byref(status), None) == capi.CPIC_EINVAL
+    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(flags=32)), C.byref(status), None) == capi.CPIC_EINVAL
+    # LayoutLeft accumulators hold real_t values, not the FP64 rows of an FP32 push
+    left64 = capi.CPIC_PUSH_ACC_LAYOUT_LEFT | capi.CPIC_PUSH_ACC_F64
+    assert push(dummy, 10, dummy, dummy, C.byref(g), C.byref(_prm(flags=left64)), C.byref(status), None) == capi.CPIC_EINVAL
     assert push(None, 10, dummy, dummy, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
     assert push(dummy, -1, dummy, dummy, C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
     # empty particle list: nothing to do, no device access
@@ -105,6 +108,8 @@ def test_field_argument_validation(lib):
     assert lib.raw("cpic_advance_b")(d, 0.1, 0.1, 0.1, C.byref(capi.make_grid(4, 4, 4, 1, 0)), 4, None) == capi.CPIC_EUNSUPPORTED
     assert lib.raw("cpic_advance_e")(None, 0.1, 0.1, 0.1, C.byref(g), 0.1, 4, None) == capi.CPIC_EINVAL
     assert lib.raw("cpic_unload_accumulator")(d, None, C.byref(g), 1.0, 1.0, 1.0, 1.0, 4, None) == capi.CPIC_EINVAL
+    assert lib.raw("cpic_unload_accumulator_left")(d, None, C.byref(g), 1.0, 1.0, 1.0, 1.0, 4, None) == capi.CPIC_EINVAL
+    assert lib.raw("cpic_unload_accumulator_left")(d, d, C.byref(g), 1.0, 1.0, 1.0, 1.0, 2, None) == capi.CPIC_EINVAL
     assert lib.raw("cpic_field_energies")(d, C.byref(g), 4, d, d, 8, None) == capi.CPIC_ESCRATCH
     assert lib.raw("cpic_energy_scratch_bytes")() > 0
 

@@ -54,6 +54,27 @@ def test_unload_accumulator(orc, g, real):
 
 @pytest.mark.parametrize("real", [np.float32, np.float64])
 @pytest.mark.parametrize("g", GRIDS)
+def test_unload_accumulator_layout_left(g, real):
+    """cpic_unload_accumulator_left reads Kokkos' LayoutLeft accumulator (the
+    Kokkos-Cuda default, src/types.h:120) and writes the LayoutRight unload's
+    jf bits: the same sums in the same order."""
+    from cabanapic_gb300 import pic
+    nx, ny, nz = g
+    f, nc = random_fields(nx, ny, nz, seed=12, real=real)
+    acc = np.random.default_rng(13).standard_normal((nc, 3, 4)).astype(real)
+    out = []
+    for layout in ("right", "left"):
+        F = _dev_fields(f, nc, real)
+        A = pic.AccumulatorArray(nc, real, layout=layout)
+        A.set(acc)
+        assert np.array_equal(A.get(), acc)
+        pic.unload_accumulator_array(F, A, nx, ny, nz, 1, real(0.3), real(0.25), real(0.2), real(0.07))
+        out.append(F.buf.cpu().numpy())
+    assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("real", [np.float32, np.float64])
+@pytest.mark.parametrize("g", GRIDS)
 def test_advance_b(orc, g, real):
     from cabanapic_gb300 import pic
     nx, ny, nz = g

@@ -253,3 +253,38 @@ def test_push_into_matches_in_place_push(orc, real, vl, acc64):
         assert np.array_equal(got[k].view(np.uint8), want[k].view(np.uint8)), k
     eps = np.finfo(real).eps
     assert np.all(np.abs(A.get().astype(np.float64) - acc) <= reorder_bound(acc_abs, cnt, eps))
+
+
+@pytest.mark.parametrize("tiles", [True, False])
+@pytest.mark.parametrize("real", [np.float32, np.float64])
+def test_push_accumulator_layout_left(orc, tiles, real):
+    """CPIC_PUSH_ACC_LAYOUT_LEFT: the accumulator in Kokkos' LayoutLeft, the
+    default layout of accumulator_array_t = View<real_t*[3][4]> in a Kokkos-Cuda
+    build of the reference (src/types.h:120, example/example.cpp:137).  The
+    particles are the LayoutRight push's bytes; the deposits, read back
+    transposed, are the oracle's within the summation-reordering bound."""
+    from cabanapic_gb300 import pic
+    st = random_state(nx=7, ny=5, nz=4, n=20011, seed=23, real=real, sort=True, crossing=0.2, disorder=0.3)
+    nc = st["num_cells"]
+    host = st["particles"].copy()
+    acc = np.zeros((nc, 3, 4), real)
+    acc_abs = np.zeros_like(acc)
+    cnt = np.zeros((nc, 3, 4), np.int32)
+    orc.push(host, st["n"], st["vl"], st["interp"], *st["push_args"], acc, st["ogrid"], acc_abs=acc_abs,
+             acc_count=cnt)
+    for exact in (True, False):
+        P = pic.ParticleList(st["n"], real, st["vl"]).upload(st["particles"])
+        I = pic.InterpolatorArray(nc, real)
+        I.buf.copy_(torch.from_numpy(st["interp"]))
+        A = pic.AccumulatorArray(nc, real, layout="left")
+        pic.push(P, I, *st["push_args"], A, None, st["nx"], st["ny"], st["nz"], 1, pic.Boundary.Periodic,
+                 exact=exact, tiles=tiles)
+        pic.check_status()
+        bound = reorder_bound(acc_abs, cnt, np.finfo(real).eps)
+        if exact:
+            assert np.array_equal(P.download_bytes(), host)
+        else:
+            assert_particles_close(P.download_bytes(), host, st["n"], real, st["vl"], st["nx"], st["ny"], st["nz"])
+            bound = bound + 1e-5 * acc_abs + 1e-6 * float(acc_abs.max())
+        err = np.abs(A.get().astype(np.float64) - acc)
+        assert np.all(err <= bound), err.max()

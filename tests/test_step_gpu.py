@@ -142,6 +142,17 @@ def test_cpp_driver_passes_reference_rule(tmp_path):
     assert np.abs(mine[:, 2:4] / g[:, 2:4] - 1).max() < 2e-5  # ostream prints 6 digits
 
 
+def test_cpp_driver_with_layout_left_accumulator(tmp_path):
+    """The C++ driver built with the accumulator in Kokkos' LayoutLeft (the
+    layout of accumulator_array_t in a Kokkos-Cuda build of the reference):
+    its energy history is the LayoutRight driver's to the 6 printed digits."""
+    right = _run_minipic(tmp_path, "minipic_f64", 400)
+    left = _run_minipic(tmp_path, "minipic_f64_left", 400)
+    a = np.array([[float(t) for t in l.split()] for l in right])[:, 2:4]
+    b = np.array([[float(t) for t in l.split()] for l in left])[:, 2:4]
+    assert np.all(history_deviation(b, a) < 1e-5)
+
+
 def test_cpp_driver_float(tmp_path, orc):
     """The real_t=float C++ driver: the linear phase matches the FP32 error
     level against the FP64 oracle."""
