@@ -340,6 +340,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-exact", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--cells", type=int, default=N_CELLS, help="cells per axis (profiling cases)")
     ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (profiling cases)")
     ap.add_argument("--workload", default="thermal", choices=["thermal", "diocotron"],
@@ -448,6 +449,19 @@ def main():
         fp64 = {"value": n * k64 * ws / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
                 "push_ms": p64, "fp32_over_fp64": (value / (n * k64 * ws / (ms64 / 1e3)))}
 
+    adjoint = None
+    if not args.no_adjoint:
+        # the adjoint configuration's two cases: forward K steps with
+        # checkpoints, then the reverse sweep (segment recompute + transposed
+        # steps); wall clock after a warm-up pair of passes
+        from cabanapic_gb300 import adjoint as adj
+        adjoint = {}
+        for case in ("two-stream", "thermal3d"):
+            r = adj.measure(case)
+            adjoint[case] = {k: r[k] for k in ("particles", "K", "checkpoint", "forward_s", "backward_s",
+                                               "backward_over_forward", "gradients")}
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, cores, ns, secs = cpu_sample_run(CPU_SAMPLE_STEPS, 1)
@@ -473,6 +487,7 @@ def main():
             "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "fp64": fp64, "exact": exact,
             "phases_ms": phases["phases_ms"], "field_phase": phases["field_phase"], "sort": phases["sort"],
             "cpu_baseline": cpu,
+            "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -220,7 +220,8 @@ def measure(case: str = "two-stream", K: int = None, checkpoint: int = 20, preci
         deck = D.thermal(n=64, ppc=16, precision=precision, num_steps=K)
         f = np.zeros((deck.num_cells, 9))
         f[:, 0] = 0.01
-        run = AdjointRun(deck, D.thermal_particles(deck), fields_init=f, checkpoint=checkpoint)
+        # particles from the seeded device loader (the host restatement's particles)
+        run = AdjointRun(deck, None, fields_init=f, checkpoint=checkpoint)
         run.forward(K)  # warm-up; not timed
         run.backward()
         run.reset()

@@ -785,6 +785,25 @@ int orc_push_omp_f64(void* particles, int64_t n, int32_t vl, const double* inter
   return threads;
 }
 
+// The threaded FP64 push with sqrt() for gamma (a true FP64 gamma; the
+// reference calls sqrtf): the forward map whose finite differences check the
+// FP64 adjoint, which differentiates sqrt.  Deterministic for a fixed thread
+// count (static schedule, copies summed in thread order).
+int orc_push_omp_sqrt_f64(void* particles, int64_t n, int32_t vl, const double* interp, double qdt_2mc,
+                          double cdt_dx, double cdt_dy, double cdt_dz, double qsp, double* acc,
+                          const orc_grid* gp, int32_t threads) {
+  ORC_GRID(gp);
+  static std::vector<double> dup;
+  orc::Particles<double> P{(unsigned char*)particles, vl};
+#ifdef _OPENMP
+  if (threads <= 0) threads = omp_get_max_threads();
+#else
+  threads = 1;
+#endif
+  orc::push_openmp<double>(P, (size_t)n, interp, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, acc, g, false, threads, dup);
+  return threads;
+}
+
 #define ORC_FIELD_FNS(T, SUF)                                                                 \
   int orc_load_interpolator_##SUF(const T* fields, T* interp, const orc_grid* gp) {          \
     ORC_GRID(gp); orc::load_interpolator<T>(fields, interp, g); return 0; }                 \

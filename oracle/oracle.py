@@ -56,6 +56,7 @@ class Oracle:
         lib.orc_uncenter_f32.argtypes = [_c_p, _i64, _i32, _c_p, _f32]
         lib.orc_uncenter_f64.argtypes = [_c_p, _i64, _i32, _c_p, _f64]
         lib.orc_num_threads.restype = _i32
+        lib.orc_push_omp_sqrt_f64.argtypes = [_c_p, _i64, _i32, _c_p, _f64, _f64, _f64, _f64, _f64, _c_p, gp, _i32]
         lib.orc_thermal_particles_f32.argtypes = [_c_p, _i64, _i32, _i64, _i64, _i64, _f64, _f32, C.c_uint64]
         lib.orc_thermal_particles_f64.argtypes = [_c_p, _i64, _i32, _i64, _i64, _i64, _f64, _f64, C.c_uint64]
 
@@ -84,8 +85,14 @@ class Oracle:
         return crossers.value
 
     def push_omp(self, particles, n, vl, interp, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, acc, g,
-                 threads=0) -> int:
-        fn = self.lib.orc_push_omp_f32 if acc.dtype == np.float32 else self.lib.orc_push_omp_f64
+                 threads=0, literal=True) -> int:
+        """Threaded push (per-thread accumulator copies, then their sum).
+        literal=False (FP64 only): sqrt() for gamma instead of the
+        reference's sqrtf."""
+        if acc.dtype == np.float32:
+            fn = self.lib.orc_push_omp_f32
+        else:
+            fn = self.lib.orc_push_omp_f64 if literal else self.lib.orc_push_omp_sqrt_f64
         return fn(_ptr(particles), n, vl, _ptr(interp), qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp,
                   _ptr(acc), C.byref(g), threads)
 

@@ -142,3 +142,46 @@ def assert_particles_close(got_bytes, ref_bytes, n, real, vl, nx, ny, nz, rtol=1
     flips = np.count_nonzero(g["cell"] != r["cell"])
     assert flips <= max(1, max_cell_flips * n), flips
     return flips
+
+
+def oracle_loss(orc, deck, packed, steps, fields_init=None, literal=True):
+    """Field energy E + B (double) after `steps` steps of the reference's step
+    sequence in the oracle, with its threaded push (deterministic for a fixed
+    thread count).  literal=False (FP64): sqrt() for gamma, the function the
+    FP64 adjoint differentiates."""
+    p = deck.derived()
+    R = deck.R
+    buf = packed.copy()
+    nc = deck.num_cells
+    g = orc.grid(deck.nx, deck.ny, deck.nz)
+    if fields_init is None:
+        fields = np.zeros(L.cell_array_bytes(nc, 9, R) // np.dtype(R).itemsize, R)
+    else:
+        fields = L.pack_cells(np.asarray(fields_init, R), R)
+    interp = np.zeros(L.cell_array_bytes(nc, 18, R) // np.dtype(R).itemsize, R)
+    acc = np.zeros((nc, 3, 4), R)
+    h = R(0.5)
+    for _ in range(steps):
+        orc.load_interpolator(fields, interp, g)
+        acc.fill(0)
+        orc.push_omp(buf, deck.num_particles, deck.vl, interp, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"],
+                     p["cdt_dz"], p["qsp"], acc, g, literal=literal)
+        orc.unload_accumulator(fields, acc, g, p["dx"], p["dy"], p["dz"], p["dt"])
+        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
+        orc.advance_e(fields, p["px"], p["py"], p["pz"], g, p["dt_eps0"])
+        orc.advance_b(fields, R(h * p["px"]), R(h * p["py"]), R(h * p["pz"]), g)
+    e = orc.energies(fields, g)
+    return float(e[2] + e[3])
+
+
+def robust_central_difference(f, x0, steps, agree=1e-5):
+    """Central differences of a piecewise-smooth f at x0 over the step sizes
+    `steps`: the loss of a PIC run jumps where a particle's face crossing
+    moves to another time step, and a difference whose +-h interval holds a
+    jump measures the jump.  Returns the mean of the first two consecutive
+    step sizes whose differences agree to `agree` relative, or raises."""
+    fd = [(f(x0 + h) - f(x0 - h)) / (2 * h) for h in steps]
+    for a, b in zip(fd, fd[1:]):
+        if abs(a - b) <= agree * max(abs(a), abs(b)):
+            return 0.5 * (a + b), fd
+    raise AssertionError(f"no two central differences agree: {list(zip(steps, fd))}")

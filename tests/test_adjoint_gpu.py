@@ -366,3 +366,85 @@ def test_fp32_adjoint_matches_fp64_gpu_adjoint(case):
     # a different (piecewise constant) path: allow a few in a thousand
     close = np.abs(u32 - u64) <= 1e-3 * np.abs(u64).max()
     assert close.mean() >= 0.995, close.mean()
+
+
+@pytest.mark.parametrize("precision,tol", [(8, 1e-5), (4, 1e-3)])
+def test_two_stream_256_cells_gradients_at_full_size(orc, precision, tol):
+    """The adjoint configuration's two-stream case at its own size: 256 cells,
+    256 particles per cell per beam (131,072 particles), checkpoints every 20
+    steps; the gradients of the field energy after K = 50 steps with respect
+    to the beam drift, the perturbation amplitude and a few initial momenta,
+    against FP64 central differences of the oracle (the reference's step in
+    FP64 with sqrt for gamma, deterministic): FP64 adjoint within 1e-5, FP32
+    adjoint within 1e-3.  The differences use steps of 1e-9 and below, where
+    two consecutive sizes agree (larger steps straddle the loss's jumps)."""
+    from cabanapic_gb300 import decks, layout as L
+    from cabanapic_gb300.adjoint import AdjointRun, two_stream_drift_gradients
+    from support import oracle_loss, robust_central_difference
+    K = 50
+
+    def setup(prec, drift=0.2, amp=1e-3):
+        d = decks.two_stream_1d(precision=prec, nx=256, ppc_per_beam=256, num_steps=K, drift=drift, amp=amp)
+        return d, decks.two_stream_1d_particles(d)
+
+    def loss(**kw):
+        d, h = setup(8, **kw)
+        return oracle_loss(orc, d, L.pack_particles(h, np.float64, 32), K, literal=False)
+
+    deck, host = setup(precision)
+    assert deck.num_particles == 131072
+    run = AdjointRun(deck, host, checkpoint=20, true_sqrt=(precision == 8), exact=True)
+    run.forward(K)
+    lam, _ = run.backward()
+    g_drift, g_amp = two_stream_drift_gradients(lam, deck, host)
+    hs = [1e-9, 5e-10, 2.5e-10, 1e-10]
+    fd_drift, _ = robust_central_difference(lambda v: loss(drift=v), 0.2, hs)
+    fd_amp, _ = robust_central_difference(lambda v: loss(amp=v), 1e-3, hs, agree=1e-4)
+    assert abs(g_drift - fd_drift) <= tol * abs(fd_drift), (g_drift, fd_drift)
+    assert abs(g_amp - fd_amp) <= tol * abs(fd_amp) + 1e-3 * tol * abs(fd_drift), (g_amp, fd_amp)
+    # individual initial momenta
+    d64, h64 = setup(8)
+    for pidx in (5, 70001, 131071):
+        def loss_u(v, pidx=pidx):
+            hp = {k: a.copy() for k, a in h64.items()}
+            hp["ux"][pidx] = v
+            return oracle_loss(orc, d64, L.pack_particles(hp, np.float64, 32), K, literal=False)
+        fd, _ = robust_central_difference(loss_u, float(h64["ux"][pidx]), [1e-8, 5e-9, 2.5e-9], agree=1e-4)
+        assert abs(lam["ux"][pidx] - fd) <= tol * max(abs(fd), 1e-3 * abs(fd_drift) / deck.num_particles), \
+            (pidx, lam["ux"][pidx], fd)
+
+
+@pytest.mark.parametrize("precision,tol", [(8, 2e-5), (4, 1e-3)])
+def test_uniform_ex_gradient_64_cubed_at_full_size(orc, precision, tol):
+    """The adjoint configuration's 3-D case at its own size: a 64^3 x 16 ppc
+    thermal plasma (4,194,304 particles), uniform initial E_x = E0 = 0.01,
+    K = 50, checkpoints every 20 steps: dL/dE0 against FP64 central
+    differences of the oracle (sqrt for gamma, deterministic; steps of 1e-10
+    and below agree, 1e-9 straddles a jump): FP64 adjoint within 2e-5, FP32
+    adjoint within 1e-3."""
+    from cabanapic_gb300 import decks, layout as L
+    from cabanapic_gb300.adjoint import AdjointRun
+    from support import oracle_loss, robust_central_difference
+    K = 50
+
+    def deck(prec):
+        return decks.thermal(n=64, ppc=16, precision=prec, num_steps=K)
+
+    def fields(d, E0):
+        f = np.zeros((d.num_cells, 9))
+        f[:, 0] = E0
+        return f
+
+    d64 = deck(8)
+    packed64 = orc.thermal_particles(d64)
+    fd, _ = robust_central_difference(
+        lambda e0: oracle_loss(orc, d64, packed64, K, fields_init=fields(d64, e0), literal=False),
+        0.01, [1e-10, 5e-11, 2.5e-11])
+    d = deck(precision)
+    host = L.unpack_particles(orc.thermal_particles(d), d.num_particles, d.R, d.vl)
+    run = AdjointRun(d, host, fields_init=fields(d, 0.01), checkpoint=20, true_sqrt=(precision == 8),
+                     exact=True)
+    run.forward(K)
+    _, lamF = run.backward()
+    g = float(_interior(lamF, 64, 64, 64)[..., 0].sum())
+    assert abs(g - fd) <= tol * abs(fd), (g, fd)
