@@ -145,6 +145,26 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
 __device__ __forceinline__ void cp_async_mbar_arrive(unsigned long long* b) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(b)) : "memory");
 }
+// Arrive and add `bytes` to the phase's expected transaction count (the
+// bulk copies that complete on this mbarrier count down by their sizes).
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+               : "memory");
+}
+// Bulk copy (the TMA engine, not the load/store pipe) of `bytes` from global
+// to shared memory, completing on mbarrier b.  Both addresses 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst_smem, const void* src, unsigned bytes,
+                                              unsigned long long* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst_smem)), "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+// Orders this thread's (and, after a __syncwarp, its warp's) earlier generic
+// shared-memory accesses before later bulk-copy writes to the same memory.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
   unsigned ok;
   asm volatile(

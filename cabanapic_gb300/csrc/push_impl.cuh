@@ -687,12 +687,126 @@ __device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __res
   }
 }
 
+#ifndef CPIC_TILE_BULK
+#define CPIC_TILE_BULK 0  // stage windows with per-element cp.async (0, faster) or bulk copies (1)
+#endif
+
+// Window staging through the bulk-copy (TMA) engine.  Each of the 9 segments
+// of wx <= 64 voxels lies in at most 3 consecutive 32-cell AoSoA blocks of
+// the interpolator array (cell arrays hold whole blocks: cpic_cell_array_bytes);
+// lane 0 copies those blocks whole (18 x 32 values each) into one of two
+// landing buffers, completing on the buffer's mbarrier, while the warp
+// transposes the previous segment from its landing buffer into window rows
+// (18 conflict-free 4-byte shared loads per 32 cells, 16-byte row stores).
+// The global reads take no load/store-pipe instructions, which the
+// consumers' gathers, deposits and particle stream need.  Measured at 128^3 x
+// 64 ppc it is not faster: the landing buffers' 14 KB per CTA take the
+// shared-memory carveout to its maximum, L1 shrinks from ~60 KB to ~28 KB,
+// and the global gathers of drifted particles, which hit L1, slow down (mean
+// push 2.51 -> 2.77 ms; with 5-chunk tiles, whose windows cover the tile,
+// 2.56 -> 2.54 ms).  Kept as a build option (CPIC_TILE_BULK=1).
+constexpr int kLandBlocks = 3;  // blocks per landing buffer
+
+// values per landing buffer
+constexpr size_t kLandElems = (size_t)kLandBlocks * 18 * kCellBlock;
+
+// Copy state of the producer's two landing buffers.
+struct LandState {
+  unsigned parity;  // bit k: parity of buffer k's next phase
+  unsigned pending;  // bit k: a phase of buffer k issued and not yet waited for
+};
+
+// Issues segment s of window w into landing buffer k (lane 0; the warp first
+// finishes its reads of that buffer).  Valid cells of the segment: [lo, hi).
+template <class R>
+__device__ __forceinline__ void land_issue(R* __restrict__ land, unsigned long long* lbar, LandState& ls,
+                                           const R* __restrict__ interp, const TileWin& w, int s, int ys,
+                                           int zs, int nc, int lane) {
+  const int k = s & 1;
+  const int a = segment_start(w, s, ys, zs);
+  const int lo = max(a, 0), hi = min(a + w.wx, nc);
+  const int blo = lo >> 5;
+  const int nb = lo < hi ? ((hi - 1) >> 5) - blo + 1 : 0;
+  __syncwarp();
+  if (lane == 0) {
+    fence_proxy_async_smem();
+    constexpr unsigned kBlk = 18 * kCellBlock * sizeof(R);
+    if (nb > 0) {
+      mbar_arrive_expect_tx(&lbar[k], (unsigned)nb * kBlk);
+      for (int j = 0; j < nb; ++j)
+        bulk_copy_g2s(land + k * kLandElems + (size_t)j * 18 * kCellBlock,
+                      interp + (size_t)(blo + j) * (18 * kCellBlock), kBlk, &lbar[k]);
+    } else {
+      mbar_arrive(&lbar[k]);
+    }
+  }
+  ls.pending |= 1u << k;
+}
+
+// Waits for segment s's landing buffer and writes the segment's window rows
+// (cells outside the array read as 0).  False if the wait gave up.
+template <class R>
+__device__ __forceinline__ bool land_transpose(R* __restrict__ buf, const R* __restrict__ land,
+                                               unsigned long long* lbar, LandState& ls, const TileWin& w,
+                                               int s, int ys, int zs, int nc, int lane) {
+  const int k = s & 1;
+  if (!warp_wait(&lbar[k], (ls.parity >> k) & 1u)) return false;
+  ls.parity ^= 1u << k;
+  ls.pending &= ~(1u << k);
+  const int a = segment_start(w, s, ys, zs);
+  const int lo = max(a, 0), hi = min(a + w.wx, nc);
+  const int base = (lo >> 5) << 5;
+  const R* lk = land + k * kLandElems;
+  for (int x = lane; x < w.wx; x += 32) {
+    const int gc = a + x;
+    R v[18];
+    if (gc >= lo && gc < hi) {
+      const int li = gc - base;
+      const R* src = lk + (li >> 5) * (18 * kCellBlock) + (li & 31);
+#pragma unroll
+      for (int m = 0; m < 18; ++m) v[m] = src[m * kCellBlock];
+    } else {
+#pragma unroll
+      for (int m = 0; m < 18; ++m) v[m] = R(0);
+    }
+    R* row = buf + (size_t)(s * w.wx + x) * kRow;
+    if constexpr (sizeof(R) == 4) {
+      float4* r4 = reinterpret_cast<float4*>(row);
+      r4[0] = make_float4(v[0], v[1], v[2], v[3]);
+      r4[1] = make_float4(v[4], v[5], v[6], v[7]);
+      r4[2] = make_float4(v[8], v[9], v[10], v[11]);
+      r4[3] = make_float4(v[12], v[13], v[14], v[15]);
+      *reinterpret_cast<float2*>(row + 16) = make_float2(v[16], v[17]);
+    } else {
+      double2* r2 = reinterpret_cast<double2*>(row);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) r2[q] = make_double2(v[2 * q], v[2 * q + 1]);
+    }
+  }
+  return true;
+}
+
+// Stages all 9 segments of window w into buf: segment s + 1's copy is in
+// flight while segment s is transposed.  False if a wait gave up.
+template <class R>
+__device__ __forceinline__ bool stage_window_bulk(R* __restrict__ buf, R* __restrict__ land,
+                                                  unsigned long long* lbar, LandState& ls,
+                                                  const R* __restrict__ interp, const TileWin& w, int ys,
+                                                  int zs, int nc, int lane) {
+  land_issue<R>(land, lbar, ls, interp, w, 0, ys, zs, nc, lane);
+  for (int s = 0; s < 9; ++s) {
+    if (s + 1 < 9) land_issue<R>(land, lbar, ls, interp, w, s + 1, ys, zs, nc, lane);
+    if (!land_transpose<R>(buf, land, lbar, ls, w, s, ys, zs, nc, lane)) return false;
+  }
+  return true;
+}
+
 constexpr int kTiledThreads = 512;                // tiled kernel: 16 warps per CTA
 constexpr int kConsumers = kTiledThreads / 32 - 1;  // warps 1..15 push; warp 0 stages windows
 
 template <class R>
 constexpr size_t tiled_dyn_smem(int wxmax) {
-  return (size_t)9 * wxmax * 2 * kRow * sizeof(R);
+  return (size_t)9 * wxmax * 2 * kRow * sizeof(R) + (CPIC_TILE_BULK ? 2 * kLandElems * sizeof(R) : 0);
 }
 
 // Cell of the lane-th sample particle of tile t (tiles of T particles).
@@ -726,7 +840,7 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
   R* const wbuf = reinterpret_cast<R*>(smem_raw);  // two windows of 9 * wxmax rows
   __shared__ MoverQueue<R> queues[kConsumers];
   __shared__ TileWin wins[2];
-  __shared__ __align__(8) unsigned long long full[2], empty[2];
+  __shared__ __align__(8) unsigned long long full[2], empty[2], lbar[2];
   const int warp = threadIdx.x >> 5;
   const LaneCtx lc = make_lane_ctx<R, VL>();
   const int cpt = kConsumers * chunks_per_warp;  // chunks per tile
@@ -737,15 +851,50 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
   const int G = gridDim.x;
   const size_t wrows = (size_t)9 * wxmax * kRow;
   if ((int)blockIdx.x >= ntiles) return;
+  R* const land = wbuf + 2 * wrows;  // bulk staging: two landing buffers after the windows
   if (threadIdx.x == 0) {
-    mbar_init(&full[0], 64);
-    mbar_init(&full[1], 64);
+    // producer lanes arrive on full twice (cp.async staging) or once (bulk staging)
+    mbar_init(&full[0], CPIC_TILE_BULK ? 32 : 64);
+    mbar_init(&full[1], CPIC_TILE_BULK ? 32 : 64);
     mbar_init(&empty[0], kConsumers);
     mbar_init(&empty[1], kConsumers);
+    mbar_init(&lbar[0], 1);
+    mbar_init(&lbar[1], 1);
   }
   __syncthreads();
 
-  if (warp == 0) {  // ---------------------------------------- producer
+  if (warp == 0 && CPIC_TILE_BULK) {  // ------------------------ producer, bulk staging
+    int s_cur = tile_sample<R, VL>(in, n, T, blockIdx.x, lc.lane);
+    int s_nxt = (int)blockIdx.x + G < ntiles ? tile_sample<R, VL>(in, n, T, blockIdx.x + G, lc.lane) : 0;
+    LandState ls{0u, 0u};
+    bool ok = true;
+    int j = 0;
+    for (int t = blockIdx.x; t < ntiles; t += G, ++j) {
+      const int b = j & 1;
+      if (j >= 2 && !warp_wait(&empty[b], (unsigned)((j >> 1) - 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      const TileWin w = window_from_samples(s_cur, lc.lane, wxmax, nc);
+      s_cur = s_nxt;
+      if (t + 2 * G < ntiles) s_nxt = tile_sample<R, VL>(in, n, T, t + 2 * G, lc.lane);
+      if (lc.lane == 0) wins[b] = w;
+      if (!stage_window_bulk<R>(wbuf + b * wrows, land, lbar, ls, interp, w, ys, zs, nc, lc.lane)) {
+        ok = false;
+        break;
+      }
+      mbar_arrive(&full[b]);
+    }
+    if (!ok) {
+      // copies still in flight land before the block exits (bounded waits)
+      for (int k = 0; k < 2; ++k)
+        if ((ls.pending >> k) & 1u) warp_wait(&lbar[k], (ls.parity >> k) & 1u);
+      if (lc.lane == 0) atomicOr(status, CPIC_STATUS_PIPELINE);
+    }
+    return;
+  }
+
+  if (warp == 0) {  // ---------------------------------------- producer, cp.async staging
     int s_cur = tile_sample<R, VL>(in, n, T, blockIdx.x, lc.lane);
     int s_nxt = (int)blockIdx.x + G < ntiles ? tile_sample<R, VL>(in, n, T, blockIdx.x + G, lc.lane) : 0;
     bool ok = true;
@@ -856,6 +1005,7 @@ struct TileShape {
 #ifndef CPIC_TILE_WXMAX
 #define CPIC_TILE_WXMAX 44  // longest window segment (voxels)
 #endif
+static_assert(CPIC_TILE_WXMAX <= 64, "a window segment must fit the 3-block landing buffers");
 inline TileShape tile_shape(const GridDev& g) {
   TileShape ts{CPIC_TILE_CHUNKS, CPIC_TILE_WXMAX};
   if (ts.wxmax > g.sx) ts.wxmax = g.sx;  // segments of one window must not overlap
