@@ -439,6 +439,25 @@ def main():
                "ms_per_step": ems / args.steps}
     del host_packed
 
+    e2e_cpp = None
+    if not args.no_e2e and WORKLOAD == "thermal":
+        # the same end-to-end measurement through the C++ push() interface
+        # (include/cpic/cabana.hpp): the reference's time loop in C++, the
+        # initial state uploaded from pinned host memory and the final state
+        # downloaded inside the timed region, energies read back every step
+        from cabanapic_gb300 import build as lib_build
+        torch.cuda.empty_cache()
+        cmd = [lib_build.MINIPIC, "thermal", str(N_CELLS), str(PPC), str(args.steps), str(max(args.warmup, 3)),
+               str(SORT_INTERVAL)]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+        if r.returncode == 0:
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+            e2e_cpp = {"value": d["pushes_per_s"], "unit": unit, "ms_per_step": d["ms"] / d["steps"],
+                       "h2d_bytes_per_step": d["h2d_bytes"] // d["steps"],
+                       "d2h_bytes_per_step": d["d2h_bytes"] // d["steps"], "path": d["path"]}
+        else:
+            e2e_cpp = {"error": (r.stderr or r.stdout).strip()[-300:]}
+
     fp64 = None
     if not args.no_fp64:
         k64 = max(2, min(args.steps, 10))
@@ -484,7 +503,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes},
-            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "fp64": fp64, "exact": exact,
+            "clocks": clocks, "e2e": e2e, "e2e_cpp": e2e_cpp, "gpu_launches": launches, "fp64": fp64, "exact": exact,
             "phases_ms": phases["phases_ms"], "field_phase": phases["field_phase"], "sort": phases["sort"],
             "cpu_baseline": cpu,
             "adjoint": adjoint,

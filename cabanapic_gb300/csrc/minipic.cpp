@@ -5,6 +5,16 @@
 // usage: minipic [num_steps] [energies_path]
 // Writes `step time E B` per step (dump_energies format).  Built once with
 // real_t = float (minipic) and once with REAL_TYPE=double (minipic_f64).
+//
+//        minipic thermal N PPC STEPS WARMUP [SORT_INTERVAL]
+// The throughput workload through the same C++ interface, end to end: a
+// uniform thermal plasma of N^3 cells x PPC particles (dx = 0.05, u_th = 0.05,
+// dt = 0.7 Courant, seeded on the device), sorted by cell every SORT_INTERVAL
+// (20) steps.  After WARMUP steps the timed region (CUDA events) uploads the
+// initial particle state from pinned host memory, runs STEPS steps through
+// push() and the field solver, reads each step's field energies back to
+// pinned host memory and downloads the final particle state.  Prints one JSON
+// line with the pushes per second.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -81,9 +91,119 @@ void init_particles(particle_list_t& particles, const Deck& d, real_t dxp, real_
                    "particles upload");
 }
 
+// The thermal workload (see the usage above).
+int run_thermal(int n, int ppc, int steps, int warmup, int sort_interval) {
+  const size_t nx = n, ny = n, nz = n, ng = 1;
+  const size_t num_cells = (nx + 2) * (ny + 2) * (nz + 2);
+  const size_t np = nx * ny * nz * (size_t)ppc;
+  const real_t c = 1, eps = 1, me = 1, n0 = 1, qsp = -1;
+  const real_t dx = 0.05, dy = dx, dz = dx, L = (real_t)(n * (double)dx);
+  const real_t dt = (real_t)(0.7 * (double)Deck::courant_length(L, L, L, nx, ny, nz) / c);
+  const real_t qdt_2mc = qsp * dt / (2 * me * c);
+  const real_t cdt_dx = c * dt / dx, cdt_dy = c * dt / dy, cdt_dz = c * dt / dz;
+  const real_t dt_eps0 = dt / eps;
+  const real_t we = (n0 * L * L * L) / (real_t)np;
+  const real_t px = c * dt / dx, py = c * dt / dy, pz = c * dt / dz;
+  cudaStream_t s = cpic::current_stream();
+
+  particle_list_t particles("particles", np), spare("sorted", np);
+  cpic_grid g = cpic::make_grid(nx, ny, nz, ng);
+  cpic::check(cpic_thermal_particles(particles.data(), (int64_t)np, ppc, &g, 0.05, we, 2024, cpic::kReal,
+                                     particle_list_t::vector_length, s),
+              "cpic_thermal_particles");
+  const size_t pbytes = particles.bytes();
+  void* h_in = nullptr;
+  void* h_out = nullptr;
+  double* h_energy = nullptr;
+  cpic::check_cuda(cudaHostAlloc(&h_in, pbytes, cudaHostAllocDefault), "cudaHostAlloc");
+  cpic::check_cuda(cudaHostAlloc(&h_out, pbytes, cudaHostAllocDefault), "cudaHostAlloc");
+  cpic::check_cuda(cudaHostAlloc((void**)&h_energy, sizeof(double) * 2 * (steps + 1), cudaHostAllocDefault),
+                   "cudaHostAlloc");
+  cpic::check_cuda(cudaMemcpyAsync(h_in, particles.data(), pbytes, cudaMemcpyDeviceToHost, s), "download");
+
+  interpolator_array_t interpolators("interpolator", num_cells);
+  accumulator_array_t accumulators("accumulator", num_cells);
+  auto scatter_add = create_scatter_view(accumulators);
+  field_array_t fields("fields", num_cells);
+  initialize_interpolator(interpolators);
+  Field_Solver<EM_Field_Solver> field_solver(fields);
+  grid_t* grid = new grid_t();
+  const size_t sort_bytes = cpic_sort_into_scratch_bytes((int64_t)np, (int64_t)num_cells, cpic::kReal,
+                                                         particle_list_t::vector_length);
+  cpic::DeviceBytes sort_scratch(sort_bytes), energy_scratch(cpic_energy_scratch_bytes()),
+      d_energy(sizeof(double) * 2 * (steps + 1));
+
+  auto step = [&](int k, bool record) {
+    load_interpolator_array(fields, interpolators, nx, ny, nz, ng);
+    clear_accumulator_array(fields, accumulators, nx, ny, nz);
+    if (sort_interval > 0 && k % sort_interval == 0) {
+      cpic::check(cpic_sort_particles_into(particles.data(), spare.data(), (int64_t)np, (int64_t)num_cells,
+                                           cpic::kReal, particle_list_t::vector_length, sort_scratch.get(),
+                                           sort_bytes, s),
+                  "cpic_sort_particles_into");
+      particles.swap(spare);
+    }
+    push(particles, interpolators, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, scatter_add, grid, nx, ny, nz, ng,
+         Periodic);
+    contribute(accumulators, scatter_add);
+    unload_accumulator_array(fields, accumulators, nx, ny, nz, ng, dx, dy, dz, dt);
+    field_solver.advance_b(fields, real_t(0.5) * px, real_t(0.5) * py, real_t(0.5) * pz, nx, ny, nz, ng);
+    field_solver.advance_e(fields, px, py, pz, nx, ny, nz, ng, dt_eps0);
+    field_solver.advance_b(fields, real_t(0.5) * px, real_t(0.5) * py, real_t(0.5) * pz, nx, ny, nz, ng);
+    if (record) {
+      double* de = static_cast<double*>(d_energy.get()) + 2 * k;
+      cpic::check(cpic_field_energies(fields.data(), &g, cpic::kReal, de, energy_scratch.get(),
+                                      energy_scratch.bytes(), s),
+                  "cpic_field_energies");
+      cpic::check_cuda(cudaMemcpyAsync(h_energy + 2 * k, de, 2 * sizeof(double), cudaMemcpyDeviceToHost, s),
+                       "energies");
+    }
+  };
+  for (int k = 0; k < warmup; ++k) step(k, false);
+  cpic::check_cuda(cudaStreamSynchronize(s), "warm-up");
+  cpic::check(cpic::read_status() == 0 ? CPIC_OK : CPIC_ECUDA, "device status after warm-up");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  cpic::check_cuda(cudaMemcpyAsync(particles.data(), h_in, pbytes, cudaMemcpyHostToDevice, s), "upload");
+  cpic::check_cuda(cudaMemsetAsync(fields.data(), 0, fields.bytes(), s), "fields reset");
+  for (int k = 0; k < steps; ++k) step(k, true);
+  cpic::check_cuda(cudaMemcpyAsync(h_out, particles.data(), pbytes, cudaMemcpyDeviceToHost, s), "download");
+  cudaEventRecord(e1, s);
+  cpic::check_cuda(cudaEventSynchronize(e1), "timed region");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  const int32_t st = cpic::read_status();
+  std::printf("{\"path\": \"C++ push() interface (include/cpic/cabana.hpp)\", \"particles\": %zu, "
+              "\"steps\": %d, \"warmup\": %d, \"ms\": %.4f, \"pushes_per_s\": %.6e, "
+              "\"h2d_bytes\": %zu, \"d2h_bytes\": %zu, \"energy_last\": [%.9e, %.9e], \"status\": %d}\n",
+              np, steps, warmup, ms, (double)np * steps / (ms * 1e-3), pbytes,
+              pbytes + sizeof(double) * 2 * (size_t)steps, h_energy[2 * (steps - 1)],
+              h_energy[2 * (steps - 1) + 1], st);
+  cudaFreeHost(h_in);
+  cudaFreeHost(h_out);
+  cudaFreeHost(h_energy);
+  delete grid;
+  return st == 0 ? 0 : 2;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
+  if (argc > 1 && std::strcmp(argv[1], "thermal") == 0) {
+    if (argc < 6) {
+      std::fprintf(stderr, "usage: minipic thermal N PPC STEPS WARMUP [SORT_INTERVAL]\n");
+      return 1;
+    }
+    try {
+      return run_thermal(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]),
+                         argc > 6 ? std::atoi(argv[6]) : 20);
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "minipic: %s\n", e.what());
+      return 1;
+    }
+  }
   Deck deck;
   const int num_steps = argc > 1 ? std::atoi(argv[1]) : deck.num_steps;
   const char* energies_path = argc > 2 ? argv[2] : "energies.txt";

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <functional>
 #include <stdexcept>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -67,6 +68,10 @@ class DeviceBytes {
   ~DeviceBytes() { if (p_) cudaFree(p_); }
   void* get() const { return p_; }
   size_t bytes() const { return n_; }
+  void swap(DeviceBytes& o) noexcept {
+    std::swap(p_, o.p_);
+    std::swap(n_, o.n_);
+  }
 
  private:
   void* p_ = nullptr;
@@ -90,6 +95,12 @@ class particle_list_t {
   size_t size() const { return n_; }
   void* data() const { return mem_.get(); }
   size_t bytes() const { return mem_.bytes(); }
+  // exchanges the storage of two lists of the same size (a double-buffered
+  // sort writes the sorted list into the second one)
+  void swap(particle_list_t& o) noexcept {
+    std::swap(n_, o.n_);
+    mem_.swap(o.mem_);
+  }
 
  private:
   size_t n_;
