@@ -153,6 +153,28 @@ def test_cpp_driver_with_layout_left_accumulator(tmp_path):
     assert np.all(history_deviation(b, a) < 1e-5)
 
 
+def test_cpp_driver_thermal_mode_runs_the_workload_end_to_end():
+    """minipic thermal: the throughput workload through the C++ push()
+    interface (seeded device loader, double-buffered sort, upload and
+    download in the timed region) on a small grid; its last field energies
+    are those of the Python time loop on the same particles, to FP32
+    summation-order noise."""
+    import json
+    from cabanapic_gb300 import build, decks
+    from cabanapic_gb300.simulation import Simulation
+    r = subprocess.run([os.path.join(build.OUT, "minipic"), "thermal", "16", "8", "25", "3", "20"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["status"] == 0 and d["particles"] == 16 ** 3 * 8 and d["pushes_per_s"] > 0
+    deck = decks.thermal(n=16, ppc=8, num_steps=25)
+    sim = Simulation(deck, sort_interval=20, max_steps=25)
+    sim.run(25)
+    sim.check_status()
+    e = sim.energies()[-1]
+    np.testing.assert_allclose(d["energy_last"], e, rtol=1e-4)
+
+
 def test_cpp_driver_float(tmp_path, orc):
     """The real_t=float C++ driver: the linear phase matches the FP32 error
     level against the FP64 oracle."""
