@@ -49,7 +49,10 @@ class AdjointRun:
         nc = deck.num_cells
         dev = self.sim.device
         self.lam_fields = FieldArray(nc, R, dev)
-        self.lam_interp = InterpolatorArray(nc, R, dev)
+        # the interpolator adjoint in cell-major rows (CPIC_ADJ_INTERP_ROWS): a
+        # particle's 18 coefficient adjoints land in one or two lines
+        self.lam_interp_rows = torch.zeros(nc * capi.CPIC_ADJ_INTERP_ROW,
+                                           dtype=torch.float32 if R == np.float32 else torch.float64, device=dev)
         self.lam_acc = AccumulatorArray(nc, R, dev)
         self.lam_part = ParticleList(deck.num_particles, R, deck.vl, dev)
         self.checkpoints = []
@@ -134,7 +137,7 @@ class AdjointRun:
         prec = self.sim.particles.precision
         stream = torch.cuda.current_stream().cuda_stream
         status = pic.status_word()
-        flags = (capi.CPIC_PUSH_TRUE_SQRT if self.true_sqrt else 0)
+        flags = (capi.CPIC_PUSH_TRUE_SQRT if self.true_sqrt else 0) | capi.CPIC_ADJ_INTERP_ROWS
         prm = capi.CpicPushParams(float(p["qdt_2mc"]), float(p["cdt_dx"]), float(p["cdt_dy"]),
                                   float(p["cdt_dz"]), float(p["qsp"]), prec, d.vl, flags, 0)
         h = d.R(0.5)
@@ -176,11 +179,12 @@ class AdjointRun:
                 lib.call("cpic_adjoint_advance_b", L.ptr, *hp, C.byref(grid), prec, stream)
                 lib.call("cpic_adjoint_unload_accumulator", L.ptr, self.lam_acc.ptr, C.byref(grid),
                          float(p["dx"]), float(p["dy"]), float(p["dz"]), float(p["dt"]), prec, stream)
-                self.lam_interp.buf.zero_()
+                self.lam_interp_rows.zero_()
                 lib.call("cpic_adjoint_push", P.data_ptr(), d.num_particles, I.data_ptr(),
-                         self.lam_acc.ptr, self.lam_part.ptr, self.lam_interp.ptr, C.byref(grid),
+                         self.lam_acc.ptr, self.lam_part.ptr, self.lam_interp_rows.data_ptr(), C.byref(grid),
                          C.byref(prm), status.data_ptr(), stream)
-                lib.call("cpic_adjoint_load_interpolator", self.lam_interp.ptr, L.ptr, C.byref(grid), prec, stream)
+                lib.call("cpic_adjoint_load_interpolator_rows", self.lam_interp_rows.data_ptr(), L.ptr,
+                         C.byref(grid), prec, stream)
         torch.cuda.synchronize()
         self.timing["backward_s"] = time.perf_counter() - t0
         pic.check_status()

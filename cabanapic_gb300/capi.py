@@ -31,6 +31,8 @@ CPIC_PUSH_EXACT = 2
 CPIC_PUSH_STREAMING = 4
 CPIC_PUSH_ACC_F64 = 8
 CPIC_PUSH_ACC_LAYOUT_LEFT = 16
+CPIC_ADJ_INTERP_ROWS = 32
+CPIC_ADJ_INTERP_ROW = 20
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -104,6 +106,7 @@ _SIGS = {
     "cpic_adjoint_unload_accumulator": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64,
                                                _i32, _vp]),
     "cpic_adjoint_load_interpolator": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _i32, _vp]),
+    "cpic_adjoint_load_interpolator_rows": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _i32, _vp]),
     "cpic_uncenter_particles": (_i32, [_vp, _i64, _vp, _f64, C.POINTER(CpicGrid), _i32, _i32, _vp, _vp]),
     "cpic_es_advance_e": (_i32, [_vp, C.POINTER(CpicGrid), _f64, _i32, _i32, _vp]),
     "cpic_es_e_energy": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _vp, _vp, _sz, _vp]),

@@ -22,6 +22,7 @@ namespace cpic {
 namespace {
 
 constexpr int kAdjThreads = 256;
+constexpr int kAdjRow = CPIC_ADJ_INTERP_ROW;  // values per row of a row-layout interpolator adjoint
 
 struct Periodic {
   GridDev g;
@@ -107,14 +108,15 @@ adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R
 // lambda_(E, B) += P^T lambda_I, P the interpolator load
 // (src/interpolator.cpp:80-131): each field value feeds the coefficients of up
 // to four cells (E) or two cells (B); gathered per field cell.
-template <class R>
+template <class R, bool ROWS = false>
 __global__ void __launch_bounds__(kAdjThreads)
 adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g, int begin, int end) {
   int j, x, y, z;
   if (!interior_cell(begin, end, g, j, x, y, z)) return;
   const Periodic P{g};
   const int xm = P.xm(x), ym = P.ym(y), zm = P.zm(z);
-  auto li = [&](int c, int m) { return LI[cell_at<18>(c, m)]; };
+  // ROWS: the interpolator adjoint in cell-major rows of kAdjRow values
+  auto li = [&](int c, int m) { return ROWS ? LI[(size_t)c * kAdjRow + m] : LI[cell_at<18>(c, m)]; };
   const R q = 0.25, h = 0.5;
   // the four weights of a bilinear coefficient block (value, d/da, d/db, d2/dadb)
   // for corners w0 (own), w1 (+a), w2 (+b), w3 (+a+b)
@@ -199,6 +201,20 @@ extern "C" int cpic_adjoint_unload_accumulator(const void* d_lambda_fields, void
         static_cast<const double*>(d_lambda_fields), static_cast<double*>(d_lambda_acc), g,
         0.25 / (dy * dz * dt), 0.25 / (dz * dx * dt), 0.25 / (dx * dy * dt), r.begin, r.end);
   }
+  return launch_status();
+}
+
+extern "C" int cpic_adjoint_load_interpolator_rows(const void* d_lambda_interp_rows, void* d_lambda_fields,
+                                                   const cpic_grid* grid, int32_t precision,
+                                                   cpic_stream_t stream) {
+  ADJ_PREAMBLE();
+  if (!d_lambda_interp_rows || !d_lambda_fields) return CPIC_EINVAL;
+  if (precision == CPIC_FLOAT)
+    adj_interp_kernel<float, true><<<r.blocks, kAdjThreads, 0, s>>>(
+        static_cast<const float*>(d_lambda_interp_rows), static_cast<float*>(d_lambda_fields), g, r.begin, r.end);
+  else
+    adj_interp_kernel<double, true><<<r.blocks, kAdjThreads, 0, s>>>(
+        static_cast<const double*>(d_lambda_interp_rows), static_cast<double*>(d_lambda_fields), g, r.begin, r.end);
   return launch_status();
 }
 

@@ -361,7 +361,26 @@ __device__ __forceinline__ int value18_of_lane(int lane) {
   return 9 * ((lane >> 4) & 1) + i2;
 }
 
-template <class R, int VL, bool LITERAL>
+// 8 consecutive bytes of float (red.global.add.v2.f32; 8-byte aligned).
+__device__ __forceinline__ void red_add2(float* a, float v0, float v1) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(a), "f"(v0), "f"(v1) : "memory");
+}
+
+// Adds the 18 coefficient adjoints of one particle to its cell's row (ROWS
+// layout): 4 x 16 + 8 bytes of vector reductions for float, scalar atomics
+// over 144 consecutive bytes for double.
+__device__ __forceinline__ void red_row18(float* row, const float v[18]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) red_add4(row + 4 * k, v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+  red_add2(row + 16, v[16], v[17]);
+}
+__device__ __forceinline__ void red_row18(double* row, const double v[18]) {
+#pragma unroll
+  for (int m = 0; m < 18; ++m) red_add(row + m, v[m]);
+}
+
+// ROWS: lambda_interp in cell-major rows of CPIC_ADJ_INTERP_ROW values.
+template <class R, int VL, bool LITERAL, bool ROWS>
 __global__ void __launch_bounds__(kAdjThreads)
 adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __restrict__ interp,
                     const R* __restrict__ lacc, unsigned char* __restrict__ lpart, R* __restrict__ linterp,
@@ -388,21 +407,31 @@ adjoint_push_kernel(const unsigned char* __restrict__ part, int n, const R* __re
     const R tot = reduce_scatter18<R>(w, lane);
     const int major_cell = __shfl_sync(kFull, cell, leader);
     const int vi = value18_of_lane(lane);
-    if (vi >= 0) red_add(linterp + cell_at<18>(major_cell, vi), tot);
+    if (vi >= 0)
+      red_add(linterp + (ROWS ? (size_t)major_cell * CPIC_ADJ_INTERP_ROW + vi : cell_at<18>(major_cell, vi)), tot);
   }
   if (dep && !in_major) {
+    if constexpr (ROWS) {
+      red_row18(linterp + (size_t)cell * CPIC_ADJ_INTERP_ROW, lf);
+    } else {
 #pragma unroll
-    for (int m = 0; m < 18; ++m) red_add(linterp + cell_at<18>(cell, m), lf[m]);
+      for (int m = 0; m < 18; ++m) red_add(linterp + cell_at<18>(cell, m), lf[m]);
+    }
   }
 }
 
 template <class R, int VL, bool LITERAL>
 int launch_adjoint(const void* part, int n, const void* interp, const void* lacc, void* lpart, void* linterp,
-                   const AdjArgs<R>& a, int* status, cudaStream_t s) {
+                   const AdjArgs<R>& a, int* status, cudaStream_t s, bool rows) {
   const unsigned blocks = (unsigned)(((int64_t)n + kAdjThreads - 1) / kAdjThreads);
-  adjoint_push_kernel<R, VL, LITERAL><<<blocks, kAdjThreads, 0, s>>>(
-      static_cast<const unsigned char*>(part), n, static_cast<const R*>(interp), static_cast<const R*>(lacc),
-      static_cast<unsigned char*>(lpart), static_cast<R*>(linterp), a, status);
+  if (rows)
+    adjoint_push_kernel<R, VL, LITERAL, true><<<blocks, kAdjThreads, 0, s>>>(
+        static_cast<const unsigned char*>(part), n, static_cast<const R*>(interp), static_cast<const R*>(lacc),
+        static_cast<unsigned char*>(lpart), static_cast<R*>(linterp), a, status);
+  else
+    adjoint_push_kernel<R, VL, LITERAL, false><<<blocks, kAdjThreads, 0, s>>>(
+        static_cast<const unsigned char*>(part), n, static_cast<const R*>(interp), static_cast<const R*>(lacc),
+        static_cast<unsigned char*>(lpart), static_cast<R*>(linterp), a, status);
   return launch_status();
 }
 
@@ -411,11 +440,12 @@ int adjoint_typed(const void* part, int n, const void* interp, const void* lacc,
                   const cpic_grid* g, const cpic_push_params* prm, int* status, cudaStream_t s) {
   AdjArgs<R> a{(R)prm->qdt_2mc, (R)prm->cdt_dx, (R)prm->cdt_dy, (R)prm->cdt_dz, (R)prm->qsp, make_grid(g)};
   const bool literal = !(prm->flags & CPIC_PUSH_TRUE_SQRT) && sizeof(R) == 8;
+  const bool rows = (prm->flags & CPIC_ADJ_INTERP_ROWS) != 0;
   if (prm->particle_vl == 32)
-    return literal ? launch_adjoint<R, 32, true>(part, n, interp, lacc, lpart, linterp, a, status, s)
-                   : launch_adjoint<R, 32, false>(part, n, interp, lacc, lpart, linterp, a, status, s);
-  return literal ? launch_adjoint<R, 16, true>(part, n, interp, lacc, lpart, linterp, a, status, s)
-                 : launch_adjoint<R, 16, false>(part, n, interp, lacc, lpart, linterp, a, status, s);
+    return literal ? launch_adjoint<R, 32, true>(part, n, interp, lacc, lpart, linterp, a, status, s, rows)
+                   : launch_adjoint<R, 32, false>(part, n, interp, lacc, lpart, linterp, a, status, s, rows);
+  return literal ? launch_adjoint<R, 16, true>(part, n, interp, lacc, lpart, linterp, a, status, s, rows)
+                 : launch_adjoint<R, 16, false>(part, n, interp, lacc, lpart, linterp, a, status, s, rows);
 }
 
 }  // namespace
@@ -432,9 +462,11 @@ extern "C" int cpic_adjoint_push(const void* particles, int64_t num_particles, c
   if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
   if (prm->precision != CPIC_FLOAT && prm->precision != CPIC_DOUBLE) return CPIC_EINVAL;
   if (prm->particle_vl != 16 && prm->particle_vl != 32) return CPIC_EINVAL;
-  if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT)) return CPIC_EINVAL;
+  if (prm->flags & ~(CPIC_PUSH_TRUE_SQRT | CPIC_PUSH_EXACT | CPIC_ADJ_INTERP_ROWS)) return CPIC_EINVAL;
   if (num_particles == 0) return CPIC_OK;
   if (!particles || !interpolators || !lambda_acc || !lambda_particles || !lambda_interp) return CPIC_EINVAL;
+  // the row layout's vector reductions need 16-byte aligned rows
+  if ((prm->flags & CPIC_ADJ_INTERP_ROWS) && ((uintptr_t)lambda_interp & 15)) return CPIC_EINVAL;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const int n = (int)num_particles;
   if (prm->precision == CPIC_FLOAT)

@@ -366,6 +366,21 @@ int cpic_adjoint_unload_accumulator(const void* d_lambda_fields, void* d_lambda_
 int cpic_adjoint_load_interpolator(const void* d_lambda_interp, void* d_lambda_fields,
                                    const cpic_grid* grid, int32_t precision, cpic_stream_t stream);
 
+/* The interpolator adjoint in cell-major rows (no counterpart in the
+ * reference): cpic_adjoint_push with CPIC_ADJ_INTERP_ROWS in prm->flags adds
+ * the adjoint of cell c's 18 coefficients (interpolator member order) into
+ * values [c * CPIC_ADJ_INTERP_ROW, c * CPIC_ADJ_INTERP_ROW + 18) of
+ * lambda_interp (num_cells rows, 16-byte aligned), instead of the
+ * interpolator's AoSoA layout: a particle's 18 adjoints then land in one or
+ * two 128-byte lines as vector reductions, where the AoSoA layout spreads them
+ * over 18 lines.  cpic_adjoint_load_interpolator_rows is the transpose of the
+ * interpolator load reading that layout; together they give the AoSoA pair's
+ * result, summed in another order. */
+#define CPIC_ADJ_INTERP_ROW 20
+#define CPIC_ADJ_INTERP_ROWS 32
+int cpic_adjoint_load_interpolator_rows(const void* d_lambda_interp_rows, void* d_lambda_fields,
+                                        const cpic_grid* grid, int32_t precision, cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- status */
 /* Clears the device status word (stream-ordered). */
 int cpic_status_clear(int32_t* d_status, cpic_stream_t stream);

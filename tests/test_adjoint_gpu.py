@@ -448,3 +448,47 @@ def test_uniform_ex_gradient_64_cubed_at_full_size(orc, precision, tol):
     _, lamF = run.backward()
     g = float(_interior(lamF, 64, 64, 64)[..., 0].sum())
     assert abs(g - fd) <= tol * abs(fd), (g, fd)
+
+
+@pytest.mark.parametrize("real", [np.float64, np.float32])
+def test_adjoint_interpolator_rows_layout(real):
+    """CPIC_ADJ_INTERP_ROWS: the push adjoint adds each cell's 18 coefficient
+    adjoints into a cell-major row instead of the interpolator's AoSoA layout,
+    and cpic_adjoint_load_interpolator_rows transposes the interpolator load
+    from that layout.  The particle adjoints are identical; the field adjoint
+    equals the AoSoA pair's to summation-order precision."""
+    from cabanapic_gb300 import capi, pic
+    st = random_state(nx=6, ny=5, nz=4, n=20000, seed=12, real=real, crossing=0.2, sort=True, disorder=0.3)
+    nc, n = st["num_cells"], st["n"]
+    rng = np.random.default_rng(6)
+    lam_p = {k: rng.standard_normal(n).astype(real) for k in ("x", "y", "z", "ux", "uy", "uz")}
+    lam_a = rng.standard_normal((nc, 3, 4)).astype(real)
+    prec = np.dtype(real).itemsize
+    grid = capi.make_grid(st["nx"], st["ny"], st["nz"])
+    out = []
+    for rows in (False, True):
+        P = pic.ParticleList(n, real, 32).upload(st["particles"])
+        I = pic.InterpolatorArray(nc, real)
+        I.buf.copy_(torch.from_numpy(st["interp"]))
+        LA = pic.AccumulatorArray(nc, real)
+        LA.set(lam_a)
+        LP = pic.ParticleList(n, real, 32).upload(dict(lam_p, w=np.zeros(n, real), cell=np.zeros(n, np.int32)))
+        flags = (capi.CPIC_PUSH_TRUE_SQRT if prec == 8 else 0) | (capi.CPIC_ADJ_INTERP_ROWS if rows else 0)
+        prm = capi.CpicPushParams(*[float(v) for v in st["push_args"]], prec, 32, flags, 0)
+        if rows:
+            LI = torch.zeros(nc * capi.CPIC_ADJ_INTERP_ROW, dtype=I.buf.dtype, device="cuda")
+            li_ptr = LI.data_ptr()
+        else:
+            LI = pic.InterpolatorArray(nc, real)
+            li_ptr = LI.ptr
+        _lib().call("cpic_adjoint_push", P.ptr, n, I.ptr, LA.ptr, LP.ptr, li_ptr, C.byref(grid), C.byref(prm),
+                    pic.status_word().data_ptr(), None)
+        pic.check_status()
+        LF = _fa(np.zeros((nc, 9)), nc, real)
+        fn = "cpic_adjoint_load_interpolator_rows" if rows else "cpic_adjoint_load_interpolator"
+        _lib().call(fn, li_ptr, LF.ptr, C.byref(grid), prec, None)
+        out.append((LP.download_bytes(), _interior(LF.get_members(), st["nx"], st["ny"], st["nz"])))
+    assert np.array_equal(out[0][0], out[1][0])
+    a, b = out[0][1].astype(np.float64), out[1][1].astype(np.float64)
+    tol = 1e-10 if real == np.float64 else 1e-4
+    assert np.abs(a - b).max() <= tol * np.abs(a).max(), np.abs(a - b).max() / np.abs(a).max()

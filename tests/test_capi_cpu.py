@@ -84,6 +84,22 @@ def test_push_argument_validation(lib):
     assert push(dummy, 10, dummy, C.c_void_p(68), C.byref(g), C.byref(_prm()), C.byref(status), None) == capi.CPIC_EINVAL
 
 
+def test_adjoint_push_argument_validation(lib):
+    from cabanapic_gb300 import capi
+    f = lib.raw("cpic_adjoint_push")
+    g = capi.make_grid(4, 4, 4)
+    status = C.c_int32(0)
+    d = C.c_void_p(64)  # never dereferenced: validation fails first
+    rows = _prm(precision=8, flags=capi.CPIC_ADJ_INTERP_ROWS)
+    # the push's accumulator flags have no adjoint
+    assert f(d, 10, d, d, d, d, C.byref(g), C.byref(_prm(flags=capi.CPIC_PUSH_ACC_F64)), C.byref(status), None) == capi.CPIC_EINVAL
+    assert f(d, 10, d, d, d, None, C.byref(g), C.byref(rows), C.byref(status), None) == capi.CPIC_EINVAL
+    # interpolator-adjoint rows must start on a 16-byte boundary
+    assert f(d, 10, d, d, d, C.c_void_p(72), C.byref(g), C.byref(rows), C.byref(status), None) == capi.CPIC_EINVAL
+    assert f(None, 0, None, None, None, None, C.byref(g), C.byref(rows), C.byref(status), None) == capi.CPIC_OK
+    assert capi.CPIC_ADJ_INTERP_ROW >= 18 and capi.CPIC_ADJ_INTERP_ROW * 4 % 16 == 0
+
+
 def test_push_into_argument_validation(lib):
     from cabanapic_gb300 import capi
     f = lib.raw("cpic_push_into")
