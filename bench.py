@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SORT_INTERVAL = 20
+SORT_AHEAD = SORT_INTERVAL // 2  # sort keys: the cells this many pushes ahead
 N_CELLS = 128
 PPC = 64
 TILES = True
@@ -175,8 +176,8 @@ def gpu_run(precision, steps, warmup, ws, host_packed=None, exact=False):
     # host_packed None: the thermal plasma is generated on the device (seeded
     # Philox, csrc/init.cu) and its initial state copied out for the other legs
     # graphs: steps that do not sort replay a captured graph of their launches
-    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup + SORT_INTERVAL,
-                     exact=exact, tiles=TILES, fields=fields, graphs=True)
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, sort_ahead=SORT_AHEAD,
+                     max_steps=steps + warmup + SORT_INTERVAL, exact=exact, tiles=TILES, fields=fields, graphs=True)
     if host_packed is None:
         host_packed = sim.particles.download_bytes()
     stream = torch.cuda.current_stream()
@@ -255,8 +256,8 @@ def e2e_run(precision, steps, warmup, host_packed, ws):
     pinned_out = torch.empty_like(pinned_in).pin_memory()
     energies_host = torch.empty((steps, 2), dtype=torch.float64).pin_memory()
     # warm-up on the same arrays (not timed), then reset the state from the host
-    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, max_steps=steps + warmup, tiles=TILES,
-                     graphs=True)
+    sim = Simulation(deck, host_packed, sort_interval=SORT_INTERVAL, sort_ahead=SORT_AHEAD,
+                     max_steps=steps + warmup, tiles=TILES, graphs=True)
     for _ in range(warmup):
         sim.step()
     sim.prepare_graphs()
@@ -330,7 +331,7 @@ def cpu_sample_run(steps, warmup, precision=4, threads=0):
 
 # ---------------------------------------------------------------- main
 def main():
-    global N_CELLS, PPC, TILES, WORKLOAD
+    global N_CELLS, PPC, TILES, WORKLOAD, SORT_AHEAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -348,14 +349,18 @@ def main():
                          "column at 128 ppc (heavy cell crossing), push + step timing only")
     ap.add_argument("--streaming", action="store_true",
                     help="streaming push kernel instead of the tiled one (comparison runs)")
+    ap.add_argument("--sort-ahead", type=int, default=SORT_INTERVAL // 2,
+                    help="sort keys: the cells this many pushes ahead (0: the current cells)")
     args = ap.parse_args()
     N_CELLS, PPC, TILES = args.cells, args.ppc, not args.streaming
+    SORT_AHEAD = args.sort_ahead
     WORKLOAD = args.workload
     ws, rank, local = _dist()
     metric = "particle-pushes/s (full step, FP32)"
     unit = "particle-pushes/s"
     workload = (f"thermal plasma {N_CELLS}^3 cells x {PPC} ppc = {N_CELLS ** 3 * PPC:,} particles, "
-                f"FP32, u_th=0.05, dt=0.7 Courant, sort every {SORT_INTERVAL} steps; full step (interp, clear, "
+                f"FP32, u_th=0.05, dt=0.7 Courant, sort every {SORT_INTERVAL} steps on the cells {SORT_AHEAD} "
+                "pushes ahead; full step (interp, clear, "
                 "push+deposit, unload, advance_b/e/b, energies)")
 
     if args.impl == "reference":
@@ -406,7 +411,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "diocotron column 96x96x64 cells, annulus 0.20<r/R<0.35 at 128 "
                                        "particles per cell of annulus volume, cB_z = 5, E x B loading "
-                                       f"from the t=0 Poisson field, dt=0.99 Courant, sort every {SORT_INTERVAL} steps",
+                                       f"from the t=0 Poisson field, dt=0.99 Courant, sort every {SORT_INTERVAL} steps on "
+                                       f"the cells {SORT_AHEAD} pushes ahead",
                            "particles": n, "cells": deck.num_cells,
                            "push_kernel": "tiled" if TILES else "streaming"},
                 "push_ms": push_ms, "push_ms_by_step": [round(t, 4) for t in res["push_ms"]],

@@ -114,6 +114,8 @@ _SIGS = {
     "cpic_field_dump_values": (_i32, [_vp, C.POINTER(CpicGrid), _i32, _f64, _f64, _vp, _vp]),
     "cpic_sort_into_scratch_bytes": (_sz, [_i64, _i64, _i32, _i32]),
     "cpic_sort_particles_into": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp, _sz, _vp]),
+    "cpic_sort_particles_ahead_into": (_i32, [_vp, _vp, _i64, C.POINTER(CpicGrid), C.POINTER(CpicPushParams),
+                                               _i32, _vp, _sz, _vp]),
     "cpic_unload_accumulator_f64": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64, _i32, _vp]),
     "cpic_unload_accumulator_left": (_i32, [_vp, _vp, C.POINTER(CpicGrid), _f64, _f64, _f64, _f64, _i32, _vp]),
     "cpic_thermal_particles": (_i32, [_vp, _i64, _i32, C.POINTER(CpicGrid), _f64, _f64, C.c_uint64, _i32,

@@ -9,8 +9,8 @@
 //        minipic thermal N PPC STEPS WARMUP [SORT_INTERVAL]
 // The throughput workload through the same C++ interface, end to end: a
 // uniform thermal plasma of N^3 cells x PPC particles (dx = 0.05, u_th = 0.05,
-// dt = 0.7 Courant, seeded on the device), sorted by cell every SORT_INTERVAL
-// (20) steps.  After WARMUP steps the timed region (CUDA events) uploads the
+// dt = 0.7 Courant, seeded on the device), sorted every SORT_INTERVAL (20)
+// steps on the cells SORT_INTERVAL/2 pushes ahead.  After WARMUP steps the timed region (CUDA events) uploads the
 // initial particle state from pinned host memory, runs STEPS steps through
 // push() and the field solver, reads each step's field energies back to
 // pinned host memory and downloads the final particle state.  Prints one JSON
@@ -132,15 +132,19 @@ int run_thermal(int n, int ppc, int steps, int warmup, int sort_interval) {
                                                          particle_list_t::vector_length);
   cpic::DeviceBytes sort_scratch(sort_bytes), energy_scratch(cpic_energy_scratch_bytes()),
       d_energy(sizeof(double) * 2 * (steps + 1));
+  cpic_push_params sort_prm{};
+  sort_prm.cdt_dx = cdt_dx; sort_prm.cdt_dy = cdt_dy; sort_prm.cdt_dz = cdt_dz;
+  sort_prm.precision = cpic::kReal;
+  sort_prm.particle_vl = particle_list_t::vector_length;
 
   auto step = [&](int k, bool record) {
     load_interpolator_array(fields, interpolators, nx, ny, nz, ng);
     clear_accumulator_array(fields, accumulators, nx, ny, nz);
     if (sort_interval > 0 && k % sort_interval == 0) {
-      cpic::check(cpic_sort_particles_into(particles.data(), spare.data(), (int64_t)np, (int64_t)num_cells,
-                                           cpic::kReal, particle_list_t::vector_length, sort_scratch.get(),
-                                           sort_bytes, s),
-                  "cpic_sort_particles_into");
+      // keyed by the cells half an interval ahead
+      cpic::check(cpic_sort_particles_ahead_into(particles.data(), spare.data(), (int64_t)np, &g, &sort_prm,
+                                                 sort_interval / 2, sort_scratch.get(), sort_bytes, s),
+                  "cpic_sort_particles_ahead_into");
       particles.swap(spare);
     }
     push(particles, interpolators, qdt_2mc, cdt_dx, cdt_dy, cdt_dz, qsp, scatter_add, grid, nx, ny, nz, ng,

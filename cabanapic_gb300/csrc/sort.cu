@@ -19,6 +19,14 @@
 // point gathers from a copy of the list in the scratch; the out-of-place one
 // (for callers with two lists) gathers straight into the second list and
 // skips that copy.
+//
+// Look-ahead keys (cpic_sort_particles_ahead_into): the key of a particle is
+// the interior cell it reaches after `steps` free-streaming pushes at its
+// current momentum (the push's displacement 2 u cdt_d / gamma per step,
+// wrapped periodically; ghost and out-of-range cells keep their own key).  A
+// list sorted on the cells half a sort interval ahead is in order midway
+// through the interval instead of at its start, so the mean spread of a
+// warp's 32 particles over cells across the interval is smaller.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -51,15 +59,51 @@ static SortPlan plan_sort(int64_t n, int64_t num_cells, int prec, int vl) {
   return p;
 }
 
+// Look-ahead key parameters: k = 2 * steps * cdt_d per axis (offset units per
+// unit of u / gamma; a cell is 2 offset units wide).
+template <class R>
+struct SortAhead {
+  R kx, ky, kz;
+  int nx, ny, nz, sx, sxy;
+};
+
+// Interior index (1..n) reached from index i by a predicted offset f.
+template <class R>
+__device__ __forceinline__ int ahead_index(int i, R f, int n) {
+  const R lim = (R)(2 * n + 1);
+  if (!(f >= -lim)) f = -lim;  // also maps NaN to -lim
+  if (!(f <= lim)) f = lim;
+  const int shift = (int)floor((f + (R)1) * (R)0.5);
+  int j = (i - 1 + shift) % n;
+  if (j < 0) j += n;
+  return j + 1;
+}
+
 // Cell key of particle p: out-of-range cells go to the last bucket; lanes
-// past the end get distinct negative keys.
-template <class R, int VL>
+// past the end get distinct negative keys.  AHEAD: the interior cell the
+// particle reaches `steps` pushes ahead.
+template <class R, int VL, bool AHEAD>
 __device__ __forceinline__ int sort_key(const unsigned char* __restrict__ part, int64_t p, int n,
-                                        int num_cells, int lane) {
+                                        int num_cells, int lane, const SortAhead<R>& a) {
   using L = PLayout<R, VL>;
   if (p >= n) return -1 - lane;
   const int c = __ldg(reinterpret_cast<const int*>(part + L::cell_off(p)));
-  return ((unsigned)c < (unsigned)num_cells) ? c : num_cells;
+  R m[6];
+  if (AHEAD) {  // loaded with the cell, before any test on it (all loads in flight together)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) m[k] = __ldg(reinterpret_cast<const R*>(part + L::off(p, k)));
+  }
+  if ((unsigned)c >= (unsigned)num_cells) return num_cells;
+  if (!AHEAD) return c;
+  const int iz = c / a.sxy;
+  const int iy = (c - iz * a.sxy) / a.sx;
+  const int ix = c - iz * a.sxy - iy * a.sx;
+  if (ix < 1 || ix > a.nx || iy < 1 || iy > a.ny || iz < 1 || iz > a.nz) return c;
+  const R rg = (R)1 / sqrt((R)1 + (m[3] * m[3] + (m[4] * m[4] + m[5] * m[5])));
+  const int jx = ahead_index<R>(ix, m[0] + a.kx * m[3] * rg, a.nx);
+  const int jy = ahead_index<R>(iy, m[1] + a.ky * m[4] * rg, a.ny);
+  const int jz = ahead_index<R>(iz, m[2] + a.kz * m[5] * rg, a.nz);
+  return jx + a.sx * jy + a.sxy * jz;
 }
 
 // Groups of equal keys among the warp's lanes: `leader` is the group's first
@@ -88,20 +132,37 @@ __device__ __forceinline__ int64_t sort_chunk0() {
   return ((int64_t)blockIdx.x * (kSortThreads / 32) + (threadIdx.x >> 5)) * kSortChunks;
 }
 
-template <class R, int VL>
+// AHEAD: the count pass also parks each key in the cell member of the output
+// list (slot p, overwritten by the gather), where the scatter pass reads it
+// back instead of recomputing it from the particle's seven members.
+template <class R, int VL, bool AHEAD>
 __global__ void __launch_bounds__(kSortThreads)
-count_kernel(const unsigned char* __restrict__ part, int n, int num_cells, int* __restrict__ counts) {
+count_kernel(const unsigned char* __restrict__ part, int n, int num_cells, int* __restrict__ counts,
+             SortAhead<R> a, unsigned char* __restrict__ key_park) {
+  using L = PLayout<R, VL>;
   const int lane = lane_id();
   const int64_t c0 = sort_chunk0();
   int key[kSortChunks];
 #pragma unroll
-  for (int k = 0; k < kSortChunks; ++k) key[k] = sort_key<R, VL>(part, (c0 + k) * 32 + lane, n, num_cells, lane);
+  for (int k = 0; k < kSortChunks; ++k) key[k] = sort_key<R, VL, AHEAD>(part, (c0 + k) * 32 + lane, n, num_cells, lane, a);
 #pragma unroll
   for (int k = 0; k < kSortChunks; ++k) {
     int leader, len, rank;
     key_group(key[k], lane, leader, len, rank);
     if (leader == lane && key[k] >= 0) atomicAdd(counts + key[k], len);
+    if (AHEAD && key[k] >= 0)
+      *reinterpret_cast<int*>(key_park + L::cell_off((c0 + k) * 32 + lane)) = key[k];
   }
+}
+
+template <class R, int VL, bool AHEAD>
+__device__ __forceinline__ int scatter_key(const unsigned char* __restrict__ part,
+                                           const unsigned char* __restrict__ key_park, int64_t p, int n,
+                                           int num_cells, int lane) {
+  using L = PLayout<R, VL>;
+  if (!AHEAD) return sort_key<R, VL, false>(part, p, n, num_cells, lane, SortAhead<R>{});
+  if (p >= n) return -1 - lane;
+  return *reinterpret_cast<const int*>(key_park + L::cell_off(p));
 }
 
 // Block-local exclusive scan of kScanTile ints; returns the tile total.
@@ -182,15 +243,16 @@ scan_add_kernel(int* __restrict__ data, int64_t n, const int* __restrict__ sums)
 }
 
 // cursor: the cell offsets, advanced as slots are taken.
-template <class R, int VL>
+template <class R, int VL, bool AHEAD>
 __global__ void __launch_bounds__(kSortThreads)
 scatter_kernel(const unsigned char* __restrict__ part, int n, int num_cells, int* __restrict__ cursor,
-               int* __restrict__ perm) {
+               int* __restrict__ perm, const unsigned char* __restrict__ key_park) {
   const int lane = lane_id();
   const int64_t c0 = sort_chunk0();
   int key[kSortChunks], leader[kSortChunks], rank[kSortChunks], base[kSortChunks];
 #pragma unroll
-  for (int k = 0; k < kSortChunks; ++k) key[k] = sort_key<R, VL>(part, (c0 + k) * 32 + lane, n, num_cells, lane);
+  for (int k = 0; k < kSortChunks; ++k)
+    key[k] = scatter_key<R, VL, AHEAD>(part, key_park, (c0 + k) * 32 + lane, n, num_cells, lane);
 #pragma unroll
   for (int k = 0; k < kSortChunks; ++k) {
     int len;
@@ -224,7 +286,7 @@ gather_kernel(const unsigned char* __restrict__ src, unsigned char* __restrict__
 // otherwise src is gathered into dst (src unchanged, no copy).
 template <class R, int VL>
 static int sort_typed(void* particles, void* dst, int n, int num_cells, const SortPlan& pl,
-                      unsigned char* sc, cudaStream_t s) {
+                      unsigned char* sc, const SortAhead<R>* ahead, cudaStream_t s) {
   int* counts = reinterpret_cast<int*>(sc + pl.counts_off);
   int* sums = reinterpret_cast<int*>(sc + pl.sums_off);
   int* perm = reinterpret_cast<int*>(sc + pl.perm_off);
@@ -234,11 +296,20 @@ static int sort_typed(void* particles, void* dst, int n, int num_cells, const So
   const int64_t warps = ((int64_t)n + 32 * kSortChunks - 1) / (32 * kSortChunks);
   const unsigned cb = (unsigned)((warps + kSortThreads / 32 - 1) / (kSortThreads / 32));
   if (cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)pl.nkeys, s) != cudaSuccess) return CPIC_ECUDA;
-  count_kernel<R, VL><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts);
+  const SortAhead<R> a = ahead ? *ahead : SortAhead<R>{};
+  unsigned char* park = static_cast<unsigned char*>(dst);  // look-ahead keys: out-of-place only
+  if (ahead && !park) return CPIC_EINVAL;
+  if (ahead)
+    count_kernel<R, VL, true><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts, a, park);
+  else
+    count_kernel<R, VL, false><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts, a, nullptr);
   scan_tiles_kernel<<<(unsigned)pl.nscan_blocks, kScanThreads, 0, s>>>(counts, pl.nkeys, sums);
   scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, pl.nscan_blocks);
   scan_add_kernel<<<(unsigned)pl.nscan_blocks, kScanThreads, 0, s>>>(counts, pl.nkeys, sums);
-  scatter_kernel<R, VL><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts, perm);
+  if (ahead)
+    scatter_kernel<R, VL, true><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts, perm, park);
+  else
+    scatter_kernel<R, VL, false><<<cb, kSortThreads, 0, s>>>(part, n, num_cells, counts, perm, nullptr);
   if (dst) {
     gather_kernel<R, VL><<<pb, kSortThreads, 0, s>>>(part, static_cast<unsigned char*>(dst), n, perm);
     return launch_status();
@@ -249,17 +320,37 @@ static int sort_typed(void* particles, void* dst, int n, int num_cells, const So
   return launch_status();
 }
 
+template <class R>
+static SortAhead<R> make_ahead(const cpic_grid* g, const cpic_push_params* prm, int steps) {
+  SortAhead<R> a;
+  a.kx = (R)(2.0 * steps * prm->cdt_dx);
+  a.ky = (R)(2.0 * steps * prm->cdt_dy);
+  a.kz = (R)(2.0 * steps * prm->cdt_dz);
+  a.nx = (int)g->nx; a.ny = (int)g->ny; a.nz = (int)g->nz;
+  a.sx = a.nx + 2;
+  a.sxy = a.sx * (a.ny + 2);
+  return a;
+}
+
+// ahead: nullptr for cell keys, else look-ahead keys on this grid.
 static int sort_dispatch(void* particles, void* dst, int64_t num_particles, int64_t num_cells,
                          int32_t precision, int32_t particle_vl, void* d_scratch, size_t need,
-                         size_t scratch_bytes, const SortPlan& pl, cudaStream_t s) {
+                         size_t scratch_bytes, const SortPlan& pl, cudaStream_t s,
+                         const cpic_grid* grid = nullptr, const cpic_push_params* prm = nullptr,
+                         int steps = 0) {
   if (scratch_bytes < need) return CPIC_ESCRATCH;
   unsigned char* sc = static_cast<unsigned char*>(d_scratch);
   const int n = (int)num_particles, nc = (int)num_cells;
-  if (precision == CPIC_FLOAT)
-    return particle_vl == 32 ? sort_typed<float, 32>(particles, dst, n, nc, pl, sc, s)
-                             : sort_typed<float, 16>(particles, dst, n, nc, pl, sc, s);
-  return particle_vl == 32 ? sort_typed<double, 32>(particles, dst, n, nc, pl, sc, s)
-                           : sort_typed<double, 16>(particles, dst, n, nc, pl, sc, s);
+  if (precision == CPIC_FLOAT) {
+    const SortAhead<float> a = grid ? make_ahead<float>(grid, prm, steps) : SortAhead<float>{};
+    const SortAhead<float>* ap = grid ? &a : nullptr;
+    return particle_vl == 32 ? sort_typed<float, 32>(particles, dst, n, nc, pl, sc, ap, s)
+                             : sort_typed<float, 16>(particles, dst, n, nc, pl, sc, ap, s);
+  }
+  const SortAhead<double> a = grid ? make_ahead<double>(grid, prm, steps) : SortAhead<double>{};
+  const SortAhead<double>* ap = grid ? &a : nullptr;
+  return particle_vl == 32 ? sort_typed<double, 32>(particles, dst, n, nc, pl, sc, ap, s)
+                           : sort_typed<double, 16>(particles, dst, n, nc, pl, sc, ap, s);
 }
 
 }  // namespace cpic
@@ -317,4 +408,34 @@ extern "C" int cpic_sort_particles_into(const void* particles, void* sorted, int
   return sort_dispatch(const_cast<void*>(particles), sorted, num_particles, num_cells, precision,
                        particle_vl, d_scratch, pl.copy_off, scratch_bytes, pl,
                        reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int cpic_sort_particles_ahead_into(const void* particles, void* sorted, int64_t num_particles,
+                                              const cpic_grid* grid, const cpic_push_params* prm,
+                                              int32_t steps_ahead, void* d_scratch, size_t scratch_bytes,
+                                              cpic_stream_t stream) {
+  if (!grid || !prm) return CPIC_EINVAL;
+  const int rc = check_grid(grid);
+  if (rc) return rc;
+  if (prm->precision != CPIC_FLOAT && prm->precision != CPIC_DOUBLE) return CPIC_EINVAL;
+  if (prm->particle_vl != 16 && prm->particle_vl != 32) return CPIC_EINVAL;
+  if (steps_ahead < 0 || steps_ahead > (1 << 20)) return CPIC_EINVAL;
+  if (!(prm->cdt_dx >= 0) || !(prm->cdt_dy >= 0) || !(prm->cdt_dz >= 0)) return CPIC_EINVAL;
+  const int64_t num_cells = (int64_t)(grid->nx + 2) * (grid->ny + 2) * (grid->nz + 2);
+  if (num_particles < 0 || num_particles > 0x7fffffffLL - 64) return CPIC_EINVAL;
+  if (num_particles == 0) return CPIC_OK;
+  if (!particles || !sorted || !d_scratch) return CPIC_EINVAL;
+  {
+    const uintptr_t bytes =
+        (uintptr_t)cpic_particle_list_bytes(num_particles, prm->precision, prm->particle_vl);
+    const uintptr_t a0 = (uintptr_t)particles, b0 = (uintptr_t)sorted;
+    if (a0 < b0 + bytes && b0 < a0 + bytes) return CPIC_EINVAL;
+  }
+  if (((uintptr_t)particles & 15) || ((uintptr_t)sorted & 15) || ((uintptr_t)d_scratch & 255))
+    return CPIC_EINVAL;
+  const SortPlan pl = plan_sort(num_particles, num_cells, prm->precision, prm->particle_vl);
+  return sort_dispatch(const_cast<void*>(particles), sorted, num_particles, num_cells, prm->precision,
+                       prm->particle_vl, d_scratch, pl.copy_off, scratch_bytes, pl,
+                       reinterpret_cast<cudaStream_t>(stream), steps_ahead ? grid : nullptr, prm,
+                       steps_ahead);
 }

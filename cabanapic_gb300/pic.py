@@ -382,12 +382,27 @@ class Sorter:
     double_buffer=True keeps a second particle buffer instead of the in-place
     sort's copy: each sort gathers into it and the list swaps buffers (same
     memory, one 2 x list-size copy less per sort).  The list's buffer object
-    changes; hold the ParticleList, not its buffer."""
+    changes; hold the ParticleList, not its buffer.
 
-    def __init__(self, particles: ParticleList, num_cells: int, double_buffer: bool = False):
+    steps_ahead > 0 (double-buffered only) keys each particle by the cell it
+    reaches that many free-streaming pushes ahead (cpic_sort_particles_ahead_into);
+    `ahead` = (grid dims (nx, ny, nz), (cdt_dx, cdt_dy, cdt_dz)) is then required."""
+
+    def __init__(self, particles: ParticleList, num_cells: int, double_buffer: bool = False,
+                 steps_ahead: int = 0, ahead=None):
         lib = capi.load()
         self.num_cells = int(num_cells)
         self.double_buffer = bool(double_buffer)
+        self.steps_ahead = int(steps_ahead)
+        if self.steps_ahead < 0:
+            raise ValueError("steps_ahead must be >= 0")
+        if self.steps_ahead:
+            if not self.double_buffer or ahead is None:
+                raise ValueError("look-ahead keys need double_buffer=True and the grid and cdt's")
+            (nx, ny, nz), cdt = ahead
+            self._grid = capi.make_grid(nx, ny, nz)
+            self._prm = capi.CpicPushParams(0.0, *[float(v) for v in cdt], 0.0, particles.precision,
+                                            particles.vl, 0, 0)
         fn = "cpic_sort_into_scratch_bytes" if self.double_buffer else "cpic_sort_scratch_bytes"
         nbytes = lib.raw(fn)(particles.n, self.num_cells, particles.precision, particles.vl)
         if nbytes == 0:
@@ -397,6 +412,12 @@ class Sorter:
 
     def __call__(self, particles: ParticleList, *, stream=None) -> None:
         lib = capi.load()
+        if self.steps_ahead:
+            lib.call("cpic_sort_particles_ahead_into", particles.ptr, self.spare.data_ptr(), particles.n,
+                     C.byref(self._grid), C.byref(self._prm), self.steps_ahead, self.scratch.data_ptr(),
+                     self.scratch.numel(), _stream(stream))
+            particles.buf, self.spare = self.spare, particles.buf
+            return
         if self.double_buffer:
             lib.call("cpic_sort_particles_into", particles.ptr, self.spare.data_ptr(), particles.n,
                      self.num_cells, particles.precision, particles.vl, self.scratch.data_ptr(),

@@ -2,7 +2,8 @@
 (example/example.cpp:216-271) on one GPU, through the C ABI.
 
 Each step: load_interpolator_array -> clear_accumulator_array -> [cell sort
-every `sort_interval` steps] -> push -> unload_accumulator_array -> advance_b(1/2)
+every `sort_interval` steps, keyed by the cells `sort_ahead` pushes ahead
+(default half the interval)] -> push -> unload_accumulator_array -> advance_b(1/2)
 -> advance_e -> advance_b(1/2) -> field energies (double, kept on the device).
 Energies are copied to the host on request.  With particle_dump / field_dump
 (open text files) the loop also writes the reference's per-step dumps
@@ -25,7 +26,7 @@ from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleLis
 
 class Simulation:
     def __init__(self, deck: D.Deck, particles=None, *, device=None, sort_interval: int = 0,
-                 max_steps: int = None, time_push: bool = False, exact: bool = False,
+                 sort_ahead: int = None, max_steps: int = None, time_push: bool = False, exact: bool = False,
                  tiles: bool = True, fields=None, particle_dump=None, field_dump=None,
                  acc_f64: bool = False, graphs: bool = False):
         self.deck = deck
@@ -52,8 +53,15 @@ class Simulation:
         if fields is not None:
             self.fields.set_members(np.asarray(fields))
         self.sort_interval = int(sort_interval)
-        self.sorter = (pic.Sorter(self.particles, nc, double_buffer=True) if self.sort_interval > 0
-                       else None)
+        # look-ahead sort keys: by default the cells half a sort interval ahead
+        if self.sort_interval > 0:
+            self.sort_ahead = self.sort_interval // 2 if sort_ahead is None else int(sort_ahead)
+            self.sorter = pic.Sorter(self.particles, nc, double_buffer=True, steps_ahead=self.sort_ahead,
+                                     ahead=((deck.nx, deck.ny, deck.nz),
+                                            (self.p["cdt_dx"], self.p["cdt_dy"], self.p["cdt_dz"])))
+        else:
+            self.sort_ahead = 0
+            self.sorter = None
         cap = max_steps if max_steps is not None else max(deck.num_steps, 1)
         self.energy = torch.zeros((cap, 2), dtype=torch.float64, device=dev)
         self.step_no = 0

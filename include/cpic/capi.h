@@ -292,6 +292,23 @@ int cpic_sort_particles_into(const void* particles, void* sorted, int64_t num_pa
                              int64_t num_cells, int32_t precision, int32_t particle_vl,
                              void* d_scratch, size_t scratch_bytes, cpic_stream_t stream);
 
+/* Out-of-place sort on look-ahead keys: each particle is keyed by the interior
+ * cell it reaches after `steps_ahead` free-streaming pushes at its current
+ * momentum (displacement 2 u cdt_d / gamma per push, from prm's cdt_dx/dy/dz;
+ * periodic wrap; a particle in a ghost cell keeps its cell as key).  Sorting
+ * every S steps with steps_ahead = S/2 leaves the list in cell order midway
+ * through the interval rather than at its start, so fewer of a warp's
+ * particles sit outside its largest same-cell group, averaged over the
+ * interval.  Any order is a valid particle list: the push's results do not
+ * depend on it, only its speed.  prm supplies precision, particle_vl and the
+ * cdt's (its other members are ignored); the grid must pass the push's grid
+ * checks.  Scratch: cpic_sort_into_scratch_bytes(num_particles, cells of
+ * grid, precision, particle_vl).  steps_ahead = 0 gives cell keys. */
+int cpic_sort_particles_ahead_into(const void* particles, void* sorted, int64_t num_particles,
+                                   const cpic_grid* grid, const cpic_push_params* prm,
+                                   int32_t steps_ahead, void* d_scratch, size_t scratch_bytes,
+                                   cpic_stream_t stream);
+
 /* ---------------------------------------------------------------- diagnostics
  * FP64 diagnostics with no counterpart in the reference (its only diagnostic
  * is the field energy): what its scheme conserves, measured.

@@ -100,6 +100,26 @@ def test_adjoint_push_argument_validation(lib):
     assert capi.CPIC_ADJ_INTERP_ROW >= 18 and capi.CPIC_ADJ_INTERP_ROW * 4 % 16 == 0
 
 
+def test_look_ahead_sort_argument_validation(lib):
+    from cabanapic_gb300 import capi
+    f = lib.raw("cpic_sort_particles_ahead_into")
+    g = capi.make_grid(4, 4, 4)
+    a, b, sc = C.c_void_p(4096), C.c_void_p(1 << 20), C.c_void_p(1 << 24)
+    ok = _prm()
+    assert f(a, b, 10, None, C.byref(ok), 5, sc, 1 << 20, None) == capi.CPIC_EINVAL
+    assert f(a, b, 10, C.byref(g), None, 5, sc, 1 << 20, None) == capi.CPIC_EINVAL
+    assert f(a, b, 10, C.byref(g), C.byref(ok), -1, sc, 1 << 20, None) == capi.CPIC_EINVAL
+    assert f(a, b, 10, C.byref(g), C.byref(_prm(cdt_dx=float("nan"))), 5, sc, 1 << 20, None) == capi.CPIC_EINVAL
+    assert f(a, b, 10, C.byref(g), C.byref(_prm(particle_vl=8)), 5, sc, 1 << 20, None) == capi.CPIC_EINVAL
+    assert f(a, a, 10, C.byref(g), C.byref(ok), 5, sc, 1 << 20, None) == capi.CPIC_EINVAL  # overlapping
+    assert f(a, b, 10, C.byref(g), C.byref(ok), 5, C.c_void_p((1 << 24) + 16), 1 << 20, None) == capi.CPIC_EINVAL
+    # scratch smaller than cpic_sort_into_scratch_bytes
+    assert f(a, b, 10, C.byref(g), C.byref(ok), 5, sc, 16, None) == capi.CPIC_ESCRATCH
+    assert f(None, None, 0, C.byref(g), C.byref(ok), 5, None, 0, None) == capi.CPIC_OK
+    refl = capi.make_grid(4, 4, 4, 1, capi.CPIC_REFLECT)
+    assert f(a, b, 10, C.byref(refl), C.byref(ok), 5, sc, 1 << 20, None) == capi.CPIC_EUNSUPPORTED
+
+
 def test_push_into_argument_validation(lib):
     from cabanapic_gb300 import capi
     f = lib.raw("cpic_push_into")

@@ -147,3 +147,71 @@ def test_sort_key_patterns(kind, real, vl):
     i0 = np.lexsort(k0[::-1])
     for x, y, z in zip(ka, kb, k0):
         assert np.array_equal(x[ia], y[ib]) and np.array_equal(x[ia], z[i0])
+
+
+def _ahead_keys(p, steps, cdt, nx, ny, nz, real):
+    """Look-ahead keys restated in numpy with the device's operation order:
+    the interior cell reached after `steps` pushes of displacement
+    2 u cdt / gamma, wrapped periodically; ghost cells keep their index and
+    out-of-range cells take the last bucket.  steps = 0: the cells (a
+    particle on a +face stays in its cell)."""
+    R = np.dtype(real).type
+    sx, sy = nx + 2, ny + 2
+    nc = sx * sy * (nz + 2)
+    c = p["cell"].astype(np.int64)
+    out_of_range = (c < 0) | (c >= nc)
+    cc = np.where(out_of_range, 0, c)
+    iz = cc // (sx * sy)
+    iy = (cc - iz * sx * sy) // sx
+    ix = cc - iz * sx * sy - iy * sx
+    interior = (ix >= 1) & (ix <= nx) & (iy >= 1) & (iy <= ny) & (iz >= 1) & (iz <= nz)
+    ux, uy, uz = p["ux"], p["uy"], p["uz"]
+    with np.errstate(all="ignore"):
+        rg = R(1) / np.sqrt(R(1) + (ux * ux + (uy * uy + uz * uz)))
+
+        def idx(i, x, u, k, n):
+            f = x + R(k) * u * rg
+            lim = R(2 * n + 1)
+            f = np.where(~(f >= -lim), -lim, f)
+            f = np.where(~(f <= lim), lim, f)
+            shift = np.floor((f + R(1)) * R(0.5)).astype(np.int64)
+            return (i - 1 + shift) % n + 1
+
+        jx = idx(ix, p["x"], ux, 2.0 * steps * cdt[0], nx)
+        jy = idx(iy, p["y"], uy, 2.0 * steps * cdt[1], ny)
+        jz = idx(iz, p["z"], uz, 2.0 * steps * cdt[2], nz)
+    key = np.where(interior, jx + sx * jy + sx * sy * jz, cc) if steps else cc
+    return np.where(out_of_range, nc, key)
+
+
+@pytest.mark.parametrize("real,vl", [(np.float32, 32), (np.float64, 16)])
+@pytest.mark.parametrize("steps", [0, 1, 7, 10])
+def test_look_ahead_sort_orders_by_predicted_cell(real, vl, steps):
+    """cpic_sort_particles_ahead_into: the output is a permutation of the
+    input whose look-ahead keys (restated in numpy) are non-decreasing; fast
+    particles wrap around the periodic grid several times; ghost and
+    out-of-range cells keep their place in the key order.  steps = 0 is the
+    cell sort."""
+    from cabanapic_gb300 import capi, layout as L, pic
+    nx, ny, nz = 9, 7, 5
+    n = 30011
+    st = random_state(nx=nx, ny=ny, nz=nz, n=n, seed=steps + 3, real=real, vl=vl, crossing=0.4)
+    host = {k: v.copy() for k, v in st["host"].items()}
+    nc = st["num_cells"]
+    host["cell"][:5] = 0                  # a ghost cell
+    host["cell"][5:9] = nc + 3           # out of range
+    host["ux"][9:12] = np.asarray([np.inf, -np.inf, np.nan], real)
+    cdt = (0.45, 0.40, 0.35)
+    P = pic.ParticleList(n, real, vl).upload(host)
+    srt = pic.Sorter(P, nc, double_buffer=True, steps_ahead=steps, ahead=((nx, ny, nz), cdt)) if steps else \
+        pic.Sorter(P, nc, double_buffer=True)
+    srt(P)
+    out = P.download()
+    keys = _ahead_keys(out, steps, cdt, nx, ny, nz, real)
+    assert np.all(np.diff(keys) >= 0)
+    if steps:
+        assert np.any(keys != np.where(out["cell"] >= nc, nc, out["cell"]))  # the keys are not the cells
+    ia, ka = _records(host)
+    ib, kb = _records(out)
+    for x, y in zip(ka, kb):
+        assert np.array_equal(x[ia], y[ib])
