@@ -226,6 +226,10 @@ def _phase_summary(res, deck, peak, steps):
     field_bytes = 324 * deck.num_cells
     achieved = field_bytes / (field_ms / 1e3) / 1e9
     n = deck.num_particles
+    # count (cell 4 B; look-ahead keys: the other 24 B of the record in, the
+    # key parked in the output list 4 B out), scatter (key 4, perm 4), gather
+    # in two passes (perm 2 x 4, record 32 in, 32 out)
+    sb = 84 + (28 if SORT_AHEAD else 0)
     return {
         "phases_ms": {"interp_clear": mean("interp_clear"), "push": mean("push"),
                       "field_solve": mean("field_solve"),
@@ -235,9 +239,9 @@ def _phase_summary(res, deck, peak, steps):
                         "basis": "324 B per ghosted cell: interp 96, clear 48, unload 60, 2x advance_b 72, "
                                  "advance_e 48 (energies excluded)"},
         "sort": {"ms_per_sort": float(np.mean(sorts)) if sorts else None, "sorts": len(sorts),
-                 "interval": SORT_INTERVAL, "bytes_per_particle_per_sort": 80,
-                 "achieved_gbs": (80 * n / (np.mean(sorts) / 1e3) / 1e9) if sorts else None,
-                 "amortised_bytes_per_particle_per_step": 80 / SORT_INTERVAL},
+                 "interval": SORT_INTERVAL, "keys_ahead": SORT_AHEAD, "bytes_per_particle_per_sort": sb,
+                 "achieved_gbs": (sb * n / (np.mean(sorts) / 1e3) / 1e9) if sorts else None,
+                 "amortised_bytes_per_particle_per_step": sb / SORT_INTERVAL},
     }
 
 
@@ -331,7 +335,7 @@ def cpu_sample_run(steps, warmup, precision=4, threads=0):
 
 # ---------------------------------------------------------------- main
 def main():
-    global N_CELLS, PPC, TILES, WORKLOAD, SORT_AHEAD
+    global N_CELLS, PPC, TILES, WORKLOAD, SORT_AHEAD, SORT_INTERVAL
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -349,11 +353,15 @@ def main():
                          "column at 128 ppc (heavy cell crossing), push + step timing only")
     ap.add_argument("--streaming", action="store_true",
                     help="streaming push kernel instead of the tiled one (comparison runs)")
-    ap.add_argument("--sort-ahead", type=int, default=SORT_INTERVAL // 2,
-                    help="sort keys: the cells this many pushes ahead (0: the current cells)")
+    ap.add_argument("--sort-interval", type=int, default=SORT_INTERVAL,
+                    help="steps between cell sorts (comparison runs)")
+    ap.add_argument("--sort-ahead", type=int, default=None,
+                    help="sort keys: the cells this many pushes ahead (default half the sort interval; "
+                         "0: the current cells)")
     args = ap.parse_args()
     N_CELLS, PPC, TILES = args.cells, args.ppc, not args.streaming
-    SORT_AHEAD = args.sort_ahead
+    SORT_INTERVAL = max(1, args.sort_interval)
+    SORT_AHEAD = SORT_INTERVAL // 2 if args.sort_ahead is None else args.sort_ahead
     WORKLOAD = args.workload
     ws, rank, local = _dist()
     metric = "particle-pushes/s (full step, FP32)"
@@ -423,8 +431,8 @@ def main():
         return
     traffic = _traffic_from_profiles()
     per_step_launches = 11  # interp, push, unload, 2x(advance_b + ghost copy), fold, ghost copy, advance_e, energies
-    # a sort adds count, 3 scan passes, scatter and gather
-    launches = args.steps * per_step_launches + 6 * len(res["sort_steps"])
+    # a sort adds count, 3 scan passes, scatter and the gather's two passes
+    launches = args.steps * per_step_launches + 7 * len(res["sort_steps"])
     phases = _phase_summary(res, deck, peak, args.steps)
 
     exact = None
