@@ -269,24 +269,26 @@ def e2e_run(precision, steps, warmup, host_packed, ws):
     sim.step_no = 0
     stream = torch.cuda.current_stream()
     _barrier(ws)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    e0, eu, es, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
     e0.record(stream)
     sim.particles.upload_pinned(pinned_in)
     sim.fields.buf.zero_()
+    eu.record(stream)
     for k in range(steps):
         sim.step()
         energies_host[k].copy_(sim.energy[k], non_blocking=True)
+    es.record(stream)
     sim.particles.download_pinned(pinned_out)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    split = {"upload_ms": e0.elapsed_time(eu), "steps_ms": eu.elapsed_time(es), "download_ms": es.elapsed_time(e1)}
     pic.check_status()
     h2d = host_packed.nbytes
     d2h = host_packed.nbytes + steps * 16
     del sim
     torch.cuda.empty_cache()
-    return dict(ms=ms, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps)
+    return dict(ms=ms, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps, split=split)
 
 
 # ---------------------------------------------------------------- CPU (oracle) arm
@@ -450,7 +452,8 @@ def main():
         ems = _barrier_max(r["ms"], ws)
         e2e = {"value": n * args.steps * ws / (ems / 1e3), "unit": unit,
                "h2d_bytes_per_step": int(r["h2d_per_step"]), "d2h_bytes_per_step": int(r["d2h_per_step"]),
-               "ms_per_step": ems / args.steps}
+               "ms_per_step": ems / args.steps,
+               "split_ms": {k: round(v, 3) for k, v in r["split"].items()}}
     del host_packed
 
     e2e_cpp = None
