@@ -123,6 +123,56 @@ __device__ __forceinline__ void streak_step(V3<R>& pos, V3<R>& rem, int& c, bool
   set_comp(pos, axis, -dir);
 }
 
+// The forward Boris step and displacement (push.h:124-182) with every
+// intermediate the reverse sweep needs.
+template <class R>
+struct BorisFwd {
+  V3<R> ha, cb, u1, c1, t, c2, u3, cu, d;
+  R g1, b0, b1, b2, P, b3, D, b4, g3, rg;
+};
+
+template <class R, bool LITERAL>
+__device__ __forceinline__ BorisFwd<R> boris_fwd(const R f[18], V3<R> x0, V3<R> u0, const AdjArgs<R>& a) {
+  const R one = 1, k = a.qdt_2mc;
+  BorisFwd<R> b;
+  b.ha = {k * ((f[0] + x0.y * f[1]) + x0.z * (f[2] + x0.y * f[3])),
+          k * ((f[4] + x0.z * f[5]) + x0.x * (f[6] + x0.z * f[7])),
+          k * ((f[8] + x0.x * f[9]) + x0.y * (f[10] + x0.x * f[11]))};
+  b.cb = {f[12] + x0.x * f[13], f[14] + x0.y * f[15], f[16] + x0.z * f[17]};
+  b.u1 = {u0.x + b.ha.x, u0.y + b.ha.y, u0.z + b.ha.z};
+  b.g1 = one + dot(b.u1, b.u1);
+  b.b0 = k / root<R, LITERAL>(b.g1);
+  b.b1 = dot(b.cb, b.cb);
+  b.b2 = (b.b0 * b.b0) * b.b1;
+  b.P = one + b.b2 * (R(1. / 3.) + b.b2 * R(2. / 15.));
+  b.b3 = b.b0 * b.P;
+  b.D = one + b.b1 * (b.b3 * b.b3);
+  b.b4 = R(2) * b.b3 / b.D;
+  b.c1 = cross(b.u1, b.cb);
+  b.t = {b.u1.x + b.b3 * b.c1.x, b.u1.y + b.b3 * b.c1.y, b.u1.z + b.b3 * b.c1.z};
+  b.c2 = cross(b.t, b.cb);
+  b.u3 = {b.u1.x + b.b4 * b.c2.x + b.ha.x, b.u1.y + b.b4 * b.c2.y + b.ha.y, b.u1.z + b.b4 * b.c2.z + b.ha.z};
+  b.g3 = one + dot(b.u3, b.u3);
+  b.rg = one / root<R, LITERAL>(b.g3);
+  b.cu = {b.u3.x * a.cdt_dx, b.u3.y * a.cdt_dy, b.u3.z * a.cdt_dz};
+  b.d = {b.cu.x * b.rg, b.cu.y * b.rg, b.cu.z * b.rg};
+  return b;
+}
+
+// A load the compiler cannot merge with an earlier load of the same address:
+// the coefficients are read again after the streak sweep instead of being
+// held in registers across it.
+__device__ __forceinline__ float reload(const float* p) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double reload(const double* p) {
+  double v;
+  asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
 // The adjoint of one particle's push.  Writes lambda_x, lambda_u in place and
 // returns the 18 interpolator adjoints of its cell in lf; false (nothing
 // written, lf unset) for a particle the kernel cannot take.
@@ -147,36 +197,16 @@ __device__ __forceinline__ bool adjoint_one(const unsigned char* __restrict__ pa
   R f[18];
 #pragma unroll
   for (int m = 0; m < 18; ++m) f[m] = __ldg(interp + cell_at<18>(cell, m));
-  // the accumulator adjoint of the particle's own cell, read with the
-  // coefficients (every streak but a crosser's later ones deposits there)
-  R la0[12];
-#pragma unroll
-  for (int m = 0; m < 12; ++m) la0[m] = __ldg(lacc + (size_t)cell * 12 + m);
 
-  // ---------------- forward recompute (push.h:124-182)
-  const V3<R> ha{k * ((f[0] + x0.y * f[1]) + x0.z * (f[2] + x0.y * f[3])),
-                 k * ((f[4] + x0.z * f[5]) + x0.x * (f[6] + x0.z * f[7])),
-                 k * ((f[8] + x0.x * f[9]) + x0.y * (f[10] + x0.x * f[11]))};
-  const V3<R> cb{f[12] + x0.x * f[13], f[14] + x0.y * f[15], f[16] + x0.z * f[17]};
-  const V3<R> u1{u0.x + ha.x, u0.y + ha.y, u0.z + ha.z};
-  const R g1 = one + dot(u1, u1);
-  const R b0 = k / root<R, LITERAL>(g1);
-  const R b1 = dot(cb, cb);
-  const R b2 = (b0 * b0) * b1;
-  const R P = one + b2 * (R(1. / 3.) + b2 * R(2. / 15.));
-  const R b3 = b0 * P;
-  const R D = one + b1 * (b3 * b3);
-  const R b4 = R(2) * b3 / D;
-  const V3<R> c1 = cross(u1, cb);
-  const V3<R> t{u1.x + b3 * c1.x, u1.y + b3 * c1.y, u1.z + b3 * c1.z};
-  const V3<R> c2 = cross(t, cb);
-  const V3<R> u3{u1.x + b4 * c2.x + ha.x, u1.y + b4 * c2.y + ha.y, u1.z + b4 * c2.z + ha.z};
-  const R g3 = one + dot(u3, u3);
-  const R rg = one / root<R, LITERAL>(g3);
-  const V3<R> cu{u3.x * a.cdt_dx, u3.y * a.cdt_dy, u3.z * a.cdt_dz};
-  const V3<R> d{cu.x * rg, cu.y * rg, cu.z * rg};
+  // ---------------- forward recompute (push.h:124-182): only the
+  // displacement is kept through the streak sweep; the Boris intermediates
+  // are recomputed after it (fewer live registers, more resident warps)
+  V3<R> d;
+  {
+    const BorisFwd<R> fw = boris_fwd<R, LITERAL>(f, x0, u0, a);
+    d = fw.d;
+  }
   const R q = w * a.qsp;
-
 
   // streak split: count the streaks (their states are replayed in reverse)
   const V3<R> np{x0.x + R(2) * d.x, x0.y + R(2) * d.y, x0.z + R(2) * d.z};
@@ -227,10 +257,7 @@ __device__ __forceinline__ bool adjoint_one(const unsigned char* __restrict__ pa
     ls = {ls.x - lrem.x, ls.y - lrem.y, ls.z - lrem.z};
     // deposit of the streak into its cell
     R la[12];
-    if (c == cell) {
-#pragma unroll
-      for (int m = 0; m < 12; ++m) la[m] = la0[m];
-    } else {
+    {
       const R* ap = lacc + (size_t)c * 12;
 #pragma unroll
       for (int m = 0; m < 12; ++m) la[m] = __ldg(ap + m);
@@ -253,6 +280,13 @@ __device__ __forceinline__ bool adjoint_one(const unsigned char* __restrict__ pa
   // lpos: adjoint of the starting offsets through the move; lrem: adjoint of d
 
   // ---------------- reverse: displacement and Boris (push.h:144-182)
+#pragma unroll
+  for (int m = 0; m < 18; ++m) f[m] = reload(interp + cell_at<18>(cell, m));
+  const BorisFwd<R> fw = boris_fwd<R, LITERAL>(f, x0, u0, a);
+  const V3<R> ha = fw.ha, cb = fw.cb, u1 = fw.u1, c1 = fw.c1, t = fw.t, c2 = fw.c2, u3 = fw.u3, cu = fw.cu;
+  const R g1 = fw.g1, b0 = fw.b0, b1 = fw.b1, b2 = fw.b2, P = fw.P, b3 = fw.b3, D = fw.D, b4 = fw.b4;
+  const R g3 = fw.g3, rg = fw.rg;
+  (void)ha;
   V3<R> lx = lpos;
   V3<R> lu3{luo.x + lrem.x * a.cdt_dx * rg, luo.y + lrem.y * a.cdt_dy * rg, luo.z + lrem.z * a.cdt_dz * rg};
   const R lrg = dot(lrem, cu);
