@@ -108,6 +108,24 @@ adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R
 // lambda_(E, B) += P^T lambda_I, P the interpolator load
 // (src/interpolator.cpp:80-131): each field value feeds the coefficients of up
 // to four cells (E) or two cells (B); gathered per field cell.
+// Four (or two) consecutive coefficients of one cell.  In the row layout a
+// bilinear block (members 4k..4k+3) is 16-byte aligned and a cB pair 8-byte
+// aligned, so each is one vector load (two for double).
+template <class R>
+struct Q4 {
+  R a, b, c, d;
+};
+__device__ __forceinline__ Q4<float> ld_q4(const float* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Q4<double> ld_q4(const double* p) {
+  const double2 v0 = *reinterpret_cast<const double2*>(p), v1 = *reinterpret_cast<const double2*>(p + 2);
+  return {v0.x, v0.y, v1.x, v1.y};
+}
+__device__ __forceinline__ float2 ld_q2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ double2 ld_q2(const double* p) { return *reinterpret_cast<const double2*>(p); }
+
 template <class R, bool ROWS = false>
 __global__ void __launch_bounds__(kAdjThreads)
 adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g, int begin, int end) {
@@ -116,14 +134,26 @@ adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g, 
   const Periodic P{g};
   const int xm = P.xm(x), ym = P.ym(y), zm = P.zm(z);
   // ROWS: the interpolator adjoint in cell-major rows of kAdjRow values
-  auto li = [&](int c, int m) { return ROWS ? LI[(size_t)c * kAdjRow + m] : LI[cell_at<18>(c, m)]; };
+  auto blk = [&](int c, int m) -> Q4<R> {
+    if constexpr (ROWS) return ld_q4(LI + (size_t)c * kAdjRow + m);
+    else return {LI[cell_at<18>(c, m)], LI[cell_at<18>(c, m + 1)], LI[cell_at<18>(c, m + 2)],
+                 LI[cell_at<18>(c, m + 3)]};
+  };
+  auto pair = [&](int c, int m, R& v0, R& v1) {
+    if constexpr (ROWS) {
+      const auto v = ld_q2(LI + (size_t)c * kAdjRow + m);
+      v0 = v.x; v1 = v.y;
+    } else {
+      v0 = LI[cell_at<18>(c, m)]; v1 = LI[cell_at<18>(c, m + 1)];
+    }
+  };
   const R q = 0.25, h = 0.5;
   // the four weights of a bilinear coefficient block (value, d/da, d/db, d2/dadb)
   // for corners w0 (own), w1 (+a), w2 (+b), w3 (+a+b)
-  auto w0 = [&](int c, int m) { return q * (li(c, m) - li(c, m + 1) - li(c, m + 2) + li(c, m + 3)); };
-  auto w1 = [&](int c, int m) { return q * (li(c, m) + li(c, m + 1) - li(c, m + 2) - li(c, m + 3)); };
-  auto w2 = [&](int c, int m) { return q * (li(c, m) - li(c, m + 1) + li(c, m + 2) - li(c, m + 3)); };
-  auto w3 = [&](int c, int m) { return q * (li(c, m) + li(c, m + 1) + li(c, m + 2) + li(c, m + 3)); };
+  auto w0 = [&](int c, int m) { const Q4<R> v = blk(c, m); return q * (v.a - v.b - v.c + v.d); };
+  auto w1 = [&](int c, int m) { const Q4<R> v = blk(c, m); return q * (v.a + v.b - v.c - v.d); };
+  auto w2 = [&](int c, int m) { const Q4<R> v = blk(c, m); return q * (v.a - v.b + v.c - v.d); };
+  auto w3 = [&](int c, int m) { const Q4<R> v = blk(c, m); return q * (v.a + v.b + v.c + v.d); };
   // ex: corners (i, i+y, i+z, i+y+z)
   fm(L, j, CPIC_F_EX) += w0(j, CPIC_I_EX) + w1(g.vox(x, ym, z), CPIC_I_EX) +
                          w2(g.vox(x, y, zm), CPIC_I_EX) + w3(g.vox(x, ym, zm), CPIC_I_EX);
@@ -134,13 +164,25 @@ adj_interp_kernel(const R* __restrict__ LI, R* __restrict__ L, const GridDev g, 
   fm(L, j, CPIC_F_EZ) += w0(j, CPIC_I_EZ) + w1(g.vox(xm, y, z), CPIC_I_EZ) +
                          w2(g.vox(x, ym, z), CPIC_I_EZ) + w3(g.vox(xm, ym, z), CPIC_I_EZ);
   // cbx: (i, i+x); cby: (i, i+y); cbz: (i, i+z)
-  fm(L, j, CPIC_F_CBX) += h * (li(j, CPIC_I_CBX) - li(j, CPIC_I_DCBXDX)) +
-                          h * (li(g.vox(xm, y, z), CPIC_I_CBX) + li(g.vox(xm, y, z), CPIC_I_DCBXDX));
-  fm(L, j, CPIC_F_CBY) += h * (li(j, CPIC_I_CBY) - li(j, CPIC_I_DCBYDY)) +
-                          h * (li(g.vox(x, ym, z), CPIC_I_CBY) + li(g.vox(x, ym, z), CPIC_I_DCBYDY));
-  fm(L, j, CPIC_F_CBZ) += h * (li(j, CPIC_I_CBZ) - li(j, CPIC_I_DCBZDZ)) +
-                          h * (li(g.vox(x, y, zm), CPIC_I_CBZ) + li(g.vox(x, y, zm), CPIC_I_DCBZDZ));
+  R a0, a1, b0, b1;
+  pair(j, CPIC_I_CBX, a0, a1);
+  pair(g.vox(xm, y, z), CPIC_I_CBX, b0, b1);
+  fm(L, j, CPIC_F_CBX) += h * (a0 - a1) + h * (b0 + b1);
+  pair(j, CPIC_I_CBY, a0, a1);
+  pair(g.vox(x, ym, z), CPIC_I_CBY, b0, b1);
+  fm(L, j, CPIC_F_CBY) += h * (a0 - a1) + h * (b0 + b1);
+  pair(j, CPIC_I_CBZ, a0, a1);
+  pair(g.vox(x, y, zm), CPIC_I_CBZ, b0, b1);
+  fm(L, j, CPIC_F_CBZ) += h * (a0 - a1) + h * (b0 + b1);
 }
+
+static_assert(CPIC_I_EY == CPIC_I_EX + 4 && CPIC_I_EZ == CPIC_I_EX + 8 && CPIC_I_EX == 0,
+              "bilinear blocks at members 0, 4, 8");
+static_assert(CPIC_I_DCBXDX == CPIC_I_CBX + 1 && CPIC_I_DCBYDY == CPIC_I_CBY + 1 &&
+                  CPIC_I_DCBZDZ == CPIC_I_CBZ + 1 && CPIC_I_CBX % 2 == 0 && CPIC_I_CBY % 2 == 0 &&
+                  CPIC_I_CBZ % 2 == 0,
+              "cB pairs at even members");
+static_assert(CPIC_ADJ_INTERP_ROW % 4 == 0, "rows of a multiple of 16 bytes");
 
 inline CellRange interior_range(const GridDev& g) { return cell_range<1, kAdjThreads>(g, g.nx, g.ny, g.nz); }
 
@@ -209,6 +251,7 @@ extern "C" int cpic_adjoint_load_interpolator_rows(const void* d_lambda_interp_r
                                                    cpic_stream_t stream) {
   ADJ_PREAMBLE();
   if (!d_lambda_interp_rows || !d_lambda_fields) return CPIC_EINVAL;
+  if ((uintptr_t)d_lambda_interp_rows & 15) return CPIC_EINVAL;  // rows are read with vector loads
   if (precision == CPIC_FLOAT)
     adj_interp_kernel<float, true><<<r.blocks, kAdjThreads, 0, s>>>(
         static_cast<const float*>(d_lambda_interp_rows), static_cast<float*>(d_lambda_fields), g, r.begin, r.end);

@@ -98,6 +98,9 @@ def test_adjoint_push_argument_validation(lib):
     assert f(d, 10, d, d, d, C.c_void_p(72), C.byref(g), C.byref(rows), C.byref(status), None) == capi.CPIC_EINVAL
     assert f(None, 0, None, None, None, None, C.byref(g), C.byref(rows), C.byref(status), None) == capi.CPIC_OK
     assert capi.CPIC_ADJ_INTERP_ROW >= 18 and capi.CPIC_ADJ_INTERP_ROW * 4 % 16 == 0
+    rows_load = lib.raw("cpic_adjoint_load_interpolator_rows")
+    assert rows_load(C.c_void_p(72), d, C.byref(g), 4, None) == capi.CPIC_EINVAL
+    assert rows_load(None, d, C.byref(g), 4, None) == capi.CPIC_EINVAL
 
 
 def test_look_ahead_sort_argument_validation(lib):
