@@ -82,6 +82,14 @@ adj_advance_e_kernel(R* __restrict__ L, const GridDev g, R px, R py, R pz, R cj,
 
 // lambda_a = U^T lambda_J, U the periodic unload (src/accumulator.cpp:71-110
 // with the jf fold); writes the 12 adjoint accumulators of every interior cell.
+__device__ __forceinline__ void st4(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void st4(double* p, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+  reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
+
 template <class R>
 __global__ void __launch_bounds__(kAdjThreads)
 adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R cx, R cy, R cz, int begin, int end) {
@@ -90,19 +98,14 @@ adj_unload_kernel(const R* __restrict__ L, R* __restrict__ A, const GridDev g, R
   const Periodic P{g};
   const int xp = P.xp(x), yp = P.yp(y), zp = P.zp(z);
   auto lj = [&](int cc, int m) { return L[cell_at<9>(cc, m)]; };
+  // the cell's 48-byte row (16-byte aligned) in three 4-value stores
   R* a = A + (size_t)c * 12;
-  a[0] = cx * lj(c, CPIC_F_JFX);
-  a[1] = cx * lj(g.vox(x, yp, z), CPIC_F_JFX);
-  a[2] = cx * lj(g.vox(x, y, zp), CPIC_F_JFX);
-  a[3] = cx * lj(g.vox(x, yp, zp), CPIC_F_JFX);
-  a[4] = cy * lj(c, CPIC_F_JFY);
-  a[5] = cy * lj(g.vox(x, y, zp), CPIC_F_JFY);
-  a[6] = cy * lj(g.vox(xp, y, z), CPIC_F_JFY);
-  a[7] = cy * lj(g.vox(xp, y, zp), CPIC_F_JFY);
-  a[8] = cz * lj(c, CPIC_F_JFZ);
-  a[9] = cz * lj(g.vox(xp, y, z), CPIC_F_JFZ);
-  a[10] = cz * lj(g.vox(x, yp, z), CPIC_F_JFZ);
-  a[11] = cz * lj(g.vox(xp, yp, z), CPIC_F_JFZ);
+  st4(a, cx * lj(c, CPIC_F_JFX), cx * lj(g.vox(x, yp, z), CPIC_F_JFX), cx * lj(g.vox(x, y, zp), CPIC_F_JFX),
+      cx * lj(g.vox(x, yp, zp), CPIC_F_JFX));
+  st4(a + 4, cy * lj(c, CPIC_F_JFY), cy * lj(g.vox(x, y, zp), CPIC_F_JFY), cy * lj(g.vox(xp, y, z), CPIC_F_JFY),
+      cy * lj(g.vox(xp, y, zp), CPIC_F_JFY));
+  st4(a + 8, cz * lj(c, CPIC_F_JFZ), cz * lj(g.vox(xp, y, z), CPIC_F_JFZ), cz * lj(g.vox(x, yp, z), CPIC_F_JFZ),
+      cz * lj(g.vox(xp, yp, z), CPIC_F_JFZ));
 }
 
 // lambda_(E, B) += P^T lambda_I, P the interpolator load
@@ -232,6 +235,7 @@ extern "C" int cpic_adjoint_unload_accumulator(const void* d_lambda_fields, void
                                                double dt, int32_t precision, cpic_stream_t stream) {
   ADJ_PREAMBLE();
   if (!d_lambda_fields || !d_lambda_acc) return CPIC_EINVAL;
+  if ((uintptr_t)d_lambda_acc & 15) return CPIC_EINVAL;  // rows written with vector stores
   if (precision == CPIC_FLOAT) {
     const float rdx = (float)dx, rdy = (float)dy, rdz = (float)dz, rdt = (float)dt;
     adj_unload_kernel<float><<<r.blocks, kAdjThreads, 0, s>>>(

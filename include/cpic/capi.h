@@ -373,7 +373,8 @@ int cpic_adjoint_advance_e(void* d_lambda_fields, double px, double py, double p
                            cpic_stream_t stream);
 
 /* lambda_acc = unload^T lambda_J: transpose of unload_accumulator_array with
- * its periodic fold (src/accumulator.cpp:45-122, src/fields.h:102-271). */
+ * its periodic fold (src/accumulator.cpp:45-122, src/fields.h:102-271).
+ * d_lambda_acc ([cell][3][4], like the accumulator) must be 16-byte aligned. */
 int cpic_adjoint_unload_accumulator(const void* d_lambda_fields, void* d_lambda_acc,
                                     const cpic_grid* grid, double dx, double dy, double dz,
                                     double dt, int32_t precision, cpic_stream_t stream);

@@ -101,6 +101,8 @@ def test_adjoint_push_argument_validation(lib):
     rows_load = lib.raw("cpic_adjoint_load_interpolator_rows")
     assert rows_load(C.c_void_p(72), d, C.byref(g), 4, None) == capi.CPIC_EINVAL
     assert rows_load(None, d, C.byref(g), 4, None) == capi.CPIC_EINVAL
+    unload_adj = lib.raw("cpic_adjoint_unload_accumulator")
+    assert unload_adj(d, C.c_void_p(72), C.byref(g), 1.0, 1.0, 1.0, 1.0, 4, None) == capi.CPIC_EINVAL
 
 
 def test_look_ahead_sort_argument_validation(lib):
