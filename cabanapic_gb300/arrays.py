@@ -25,6 +25,27 @@ def _torch_real(real: np.dtype):
 _COPY_STREAMS = {}
 
 
+def copy_streams(dev, pieces: int) -> list:
+    """`pieces` side streams for host <-> device copies (created once)."""
+    streams = _COPY_STREAMS.get(dev)
+    if streams is None or len(streams) < pieces:
+        streams = [torch.cuda.Stream(dev) for _ in range(pieces)]
+        _COPY_STREAMS[dev] = streams
+    return streams
+
+
+def block_pieces(n: int, vl: int, pieces: int) -> list:
+    """Splits n particles into at most `pieces` runs of whole AoSoA blocks:
+    [(start, count)]."""
+    blocks = -(-n // vl)
+    per = -(-blocks // max(1, pieces))
+    out = []
+    for b0 in range(0, blocks, per):
+        start = b0 * vl
+        out.append((start, min(n, (b0 + per) * vl) - start))
+    return out
+
+
 def copy_in_pieces(dst: torch.Tensor, src: torch.Tensor, pieces: int = 8) -> None:
     """dst.copy_(src) between pinned host and device memory as `pieces`
     asynchronous copies on side streams, so that several copy engines move
@@ -33,10 +54,7 @@ def copy_in_pieces(dst: torch.Tensor, src: torch.Tensor, pieces: int = 8) -> Non
     assert dst.numel() == src.numel() and dst.dtype == src.dtype
     dev = dst.device if dst.is_cuda else src.device
     cur = torch.cuda.current_stream(dev)
-    streams = _COPY_STREAMS.get(dev)
-    if streams is None or len(streams) < pieces:
-        streams = [torch.cuda.Stream(dev) for _ in range(pieces)]
-        _COPY_STREAMS[dev] = streams
+    streams = copy_streams(dev, pieces)
     n = dst.numel()
     step = -(-n // pieces)
     start = torch.cuda.Event()
@@ -95,6 +113,19 @@ class ParticleList:
         complete once the current stream has reached this point."""
         copy_in_pieces(pinned, self.buf[: self.nbytes], pieces)
         return pinned
+
+    def view(self, start: int, count: int) -> "ParticleList":
+        """Particles [start, start + count) as a particle list sharing this
+        list's memory (start a multiple of the vector length, so the view is
+        whole AoSoA blocks)."""
+        if start % self.vl or start < 0 or count < 0 or start + count > self.n:
+            raise ValueError("a view starts on an AoSoA block and lies inside the list")
+        v = ParticleList.__new__(ParticleList)
+        v.n, v.real, v.vl = int(count), self.real, self.vl
+        v.nbytes = L.particle_list_bytes(v.n, self.real, self.vl)
+        off = (start // self.vl) * L.particle_block_bytes(self.real, self.vl)
+        v.buf = self.buf[off: off + max(v.nbytes, 16)]
+        return v
 
     def download_bytes(self) -> np.ndarray:
         return self.buf[: self.nbytes].cpu().numpy()

@@ -21,7 +21,8 @@ import torch
 
 from . import decks as D
 from . import pic
-from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleList
+from . import layout as L
+from .arrays import AccumulatorArray, FieldArray, InterpolatorArray, ParticleList, block_pieces, copy_streams
 
 
 class Simulation:
@@ -118,9 +119,12 @@ class Simulation:
             self._pending_step = self.step_no + 1  # the reference's loop counts steps from 1
         self.step_no += 1
 
-    def _launch_step(self, sorted_now: bool, ev, energy_out) -> None:
+    def _launch_step(self, sorted_now: bool, ev, energy_out, pieces=None) -> None:
         """The step's launches on the current stream (ev: 5 events between the
-        phases, or None; energy_out: the energies' device slot, or None)."""
+        phases, or None; energy_out: the energies' device slot, or None).
+        pieces: push the list as runs [(start, count, before, after)] of whole
+        AoSoA blocks, calling before() ahead of each run's push and after()
+        behind it (stream hooks for overlapped host copies)."""
         d, p = self.deck, self.p
         nx, ny, nz, ng = d.nx, d.ny, d.nz, d.num_ghosts
         if ev:
@@ -136,9 +140,15 @@ class Simulation:
         if self.time_push and not ev:
             ev_push = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev_push[0].record()
-        pic.push(self.particles, self.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
-                 p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary, exact=self.exact,
-                 tiles=self.tiles)
+        for start, count, before, after in (pieces or [(0, self.particles.n, None, None)]):
+            if before is not None:
+                before()
+            part = self.particles if pieces is None else self.particles.view(start, count)
+            pic.push(part, self.interpolators, p["qdt_2mc"], p["cdt_dx"], p["cdt_dy"], p["cdt_dz"],
+                     p["qsp"], self.accumulators, None, nx, ny, nz, ng, d.boundary, exact=self.exact,
+                     tiles=self.tiles)
+            if after is not None:
+                after()
         if ev:
             ev[3].record()
             if self.time_push:
@@ -209,6 +219,94 @@ class Simulation:
     def run(self, steps: int) -> None:
         for _ in range(steps):
             self.step()
+
+    def run_from_host(self, pinned_in: torch.Tensor, steps: int, pinned_out: torch.Tensor = None,
+                      energies_out: torch.Tensor = None, pieces: int = 8) -> None:
+        """Uploads the particle list from pinned host memory (its AoSoA bytes),
+        runs `steps` steps and, with pinned_out, downloads the final list; each
+        step's energies go to energies_out (pinned [steps, 2] double) if given.
+        Everything is ordered on the current stream: synchronise it before
+        reading the host buffers.
+
+        The list moves in `pieces` runs of whole AoSoA blocks on side streams.
+        Unless the first step sorts (a sort needs the whole list), its push
+        takes each run as soon as that run has landed; the last step's push
+        hands each run to its copy back as soon as it has pushed it.  Only the
+        order of the accumulator sums differs from upload, run, download."""
+        if steps < 1:
+            raise ValueError("steps must be >= 1")
+        dev = self.particles.buf.device
+        cur = torch.cuda.current_stream(dev)
+        runs = block_pieces(self.particles.n, self.particles.vl, pieces)
+        streams = copy_streams(dev, len(runs))
+        blk = L.particle_block_bytes(self.particles.real, self.particles.vl)
+        sorts_first = self.sorter is not None and self.step_no % self.sort_interval == 0
+        if self._pdump is not None or self._fdump is not None or self.time_phases or self.time_push:
+            # dumps and timing events take the plain path: upload, steps, download
+            self.particles.upload_pinned(pinned_in, pieces)
+            for k in range(steps):
+                self.step()
+                if energies_out is not None and self.step_no - 1 < self.energy.shape[0]:
+                    energies_out[k].copy_(self.energy[self.step_no - 1], non_blocking=True)
+            if pinned_out is not None:
+                self.particles.download_pinned(pinned_out, pieces)
+            return
+        if sorts_first:
+            self.particles.upload_pinned(pinned_in, pieces)
+            up = None
+        else:
+            up = []
+            ready = torch.cuda.Event()
+            ready.record(cur)
+            for (start, count), st in zip(runs, streams):
+                a, b = (start // self.particles.vl) * blk, L.particle_list_bytes(start + count, self.particles.real,
+                                                                                 self.particles.vl)
+                st.wait_event(ready)
+                with torch.cuda.stream(st):
+                    self.particles.buf[a:b].copy_(pinned_in[a:b], non_blocking=True)
+                self.particles.buf.record_stream(st)
+                done = torch.cuda.Event()
+                done.record(st)
+                up.append(done)
+
+        def download_hooks():
+            hooks = []
+            for (start, count), st in zip(runs, streams):
+                def after(start=start, count=count, st=st):
+                    a = (start // self.particles.vl) * blk
+                    b = L.particle_list_bytes(start + count, self.particles.real, self.particles.vl)
+                    pushed = torch.cuda.Event()
+                    pushed.record(cur)
+                    st.wait_event(pushed)
+                    buf = self.particles.buf  # the list's buffer after this step's sort
+                    with torch.cuda.stream(st):
+                        pinned_out[a:b].copy_(buf[a:b], non_blocking=True)
+                    buf.record_stream(st)
+                hooks.append(after)
+            return hooks
+
+        for k in range(steps):
+            last = k == steps - 1
+            special = (k == 0 and up is not None) or (last and pinned_out is not None)
+            if not special:
+                self.step()
+            else:
+                before = [(lambda e=e: cur.wait_event(e)) for e in up] if (k == 0 and up is not None) \
+                    else [None] * len(runs)
+                after = download_hooks() if (last and pinned_out is not None) else [None] * len(runs)
+                sorted_now = self.sorter is not None and self.step_no % self.sort_interval == 0
+                out = self.energy[self.step_no] if self.step_no < self.energy.shape[0] else None
+                self._launch_step(sorted_now, None, out,
+                                  pieces=[(s0, c0, bf, af) for (s0, c0), bf, af in zip(runs, before, after)])
+                self._warm = True
+                self.step_no += 1
+            if energies_out is not None and self.step_no - 1 < self.energy.shape[0]:
+                energies_out[k].copy_(self.energy[self.step_no - 1], non_blocking=True)
+        if pinned_out is not None:
+            for st in streams:
+                done = torch.cuda.Event()
+                done.record(st)
+                cur.wait_event(done)
 
     # ------------------------------------------------------------------
     def energies(self) -> np.ndarray:
