@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 
 SORT_INTERVAL = 20
 SORT_AHEAD = SORT_INTERVAL // 2  # sort keys: the cells this many pushes ahead
+E2E_RUNS = 3  # timed end-to-end runs; the median is reported
 N_CELLS = 128
 PPC = 64
 TILES = True
@@ -267,25 +268,42 @@ def e2e_run(precision, steps, warmup, host_packed, ws):
         sim.step()
     sim.prepare_graphs()
     torch.cuda.synchronize()
-    # the seeded list is in cell order, where look-ahead keys put a list
-    # halfway through a sort interval: the run starts there (its first step
-    # does not sort, so its push can start on the first pieces to land)
-    sim.step_no = SORT_INTERVAL // 2 if SORT_AHEAD else 0
     stream = torch.cuda.current_stream()
-    _barrier(ws)
-    e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
-    e0.record(stream)
-    sim.fields.buf.zero_()
-    sim.run_from_host(pinned_in, steps, pinned_out, energies_host)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    # Three timed runs from the same host state; the median is reported.  The
+    # host link is shared with the rest of the machine: single copies of the
+    # list have been seen at 35-190 GB/s against the usual 210 GB/s.
+    samples = []
+    for _ in range(E2E_RUNS):
+        # the seeded list is in cell order, where look-ahead keys put a list
+        # halfway through a sort interval: the run starts there (its first
+        # step does not sort, so its push can start on the first pieces)
+        sim.step_no = SORT_INTERVAL // 2 if SORT_AHEAD else 0
+        _barrier(ws)
+        e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+        e0.record(stream)
+        sim.fields.buf.zero_()
+        sim.run_from_host(pinned_in, steps, pinned_out, energies_host)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        samples.append(e0.elapsed_time(e1))
+    ms = float(np.median(samples))
     pic.check_status()
+    # the host link's rate right after the timed region (outside it): one
+    # upload and one download of the list alone
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(stream)
+    sim.particles.upload_pinned(pinned_in)
+    ev[1].record(stream)
+    sim.particles.download_pinned(pinned_out)
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    link = {"h2d_gbs": host_packed.nbytes / ev[0].elapsed_time(ev[1]) / 1e6,
+            "d2h_gbs": host_packed.nbytes / ev[1].elapsed_time(ev[2]) / 1e6}
     h2d = host_packed.nbytes
     d2h = host_packed.nbytes + steps * 16
     del sim
     torch.cuda.empty_cache()
-    return dict(ms=ms, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps)
+    return dict(ms=ms, h2d_per_step=h2d / steps, d2h_per_step=d2h / steps, link=link, samples=samples)
 
 
 # ---------------------------------------------------------------- CPU (oracle) arm
@@ -450,7 +468,9 @@ def main():
         e2e = {"value": n * args.steps * ws / (ems / 1e3), "unit": unit,
                "h2d_bytes_per_step": int(r["h2d_per_step"]), "d2h_bytes_per_step": int(r["d2h_per_step"]),
                "ms_per_step": ems / args.steps,
-               "path": "Simulation.run_from_host (8 pieces; first push and last download overlapped)"}
+               "path": "Simulation.run_from_host (8 pieces; first push and last download overlapped)",
+               "host_link_after_gbs": {k: round(v, 1) for k, v in r["link"].items()},
+               "runs_ms": [round(t, 3) for t in r["samples"]], "of_runs": "median"}
     del host_packed
 
     e2e_cpp = None
