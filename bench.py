@@ -488,7 +488,8 @@ def main():
             d = json.loads(r.stdout.strip().splitlines()[-1])
             e2e_cpp = {"value": d["pushes_per_s"], "unit": unit, "ms_per_step": d["ms"] / d["steps"],
                        "h2d_bytes_per_step": d["h2d_bytes"] // d["steps"],
-                       "d2h_bytes_per_step": d["d2h_bytes"] // d["steps"], "path": d["path"]}
+                       "d2h_bytes_per_step": d["d2h_bytes"] // d["steps"], "path": d["path"],
+                       "runs_ms": d.get("runs_ms"), "of_runs": "median"}
         else:
             e2e_cpp = {"error": (r.stderr or r.stdout).strip()[-300:]}
 
