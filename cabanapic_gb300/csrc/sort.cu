@@ -61,22 +61,27 @@ static SortPlan plan_sort(int64_t n, int64_t num_cells, int prec, int vl) {
 }
 
 // Look-ahead key parameters: k = 2 * steps * cdt_d per axis (offset units per
-// unit of u / gamma; a cell is 2 offset units wide).
+// unit of u / gamma; a cell is 2 offset units wide); the ghosted row and plane
+// extents with their multiply-shift divisors.
 template <class R>
 struct SortAhead {
   R kx, ky, kz;
-  int nx, ny, nz, sx, sxy;
+  int nx, ny, nz, sx, sy;
+  DivMagic dsx, dsy;
 };
 
-// Interior index (1..n) reached from index i by a predicted offset f.
+// Interior index (1..n) reached from index i by a predicted offset f.  The
+// offset is clamped to +-(2n - 1) (also NaN, to -(2n - 1)), so the shift lies
+// in [1 - n, n] and one correction wraps it periodically; a particle that
+// would cross the whole grid takes some cell of it, which any order allows.
 template <class R>
 __device__ __forceinline__ int ahead_index(int i, R f, int n) {
-  const R lim = (R)(2 * n + 1);
-  if (!(f >= -lim)) f = -lim;  // also maps NaN to -lim
+  const R lim = (R)(2 * n - 1);
+  if (!(f >= -lim)) f = -lim;
   if (!(f <= lim)) f = lim;
-  const int shift = (int)floor((f + (R)1) * (R)0.5);
-  int j = (i - 1 + shift) % n;
+  int j = i - 1 + (int)floor((f + (R)1) * (R)0.5);
   if (j < 0) j += n;
+  if (j >= n) j -= n;
   return j + 1;
 }
 
@@ -96,15 +101,15 @@ __device__ __forceinline__ int sort_key(const unsigned char* __restrict__ part, 
   }
   if ((unsigned)c >= (unsigned)num_cells) return num_cells;
   if (!AHEAD) return c;
-  const int iz = c / a.sxy;
-  const int iy = (c - iz * a.sxy) / a.sx;
-  const int ix = c - iz * a.sxy - iy * a.sx;
+  int ix = c, iy, iz;  // RANK_TO_INDEX by multiply-shift division
+  iy = div_magic(ix, a.dsx); ix -= iy * a.sx;
+  iz = div_magic(iy, a.dsy); iy -= iz * a.sy;
   if (ix < 1 || ix > a.nx || iy < 1 || iy > a.ny || iz < 1 || iz > a.nz) return c;
   const R rg = (R)1 / sqrt((R)1 + (m[3] * m[3] + (m[4] * m[4] + m[5] * m[5])));
   const int jx = ahead_index<R>(ix, m[0] + a.kx * m[3] * rg, a.nx);
   const int jy = ahead_index<R>(iy, m[1] + a.ky * m[4] * rg, a.ny);
   const int jz = ahead_index<R>(iz, m[2] + a.kz * m[5] * rg, a.nz);
-  return jx + a.sx * jy + a.sxy * jz;
+  return jx + a.sx * (jy + a.sy * jz);
 }
 
 // Groups of equal keys among the warp's lanes: `leader` is the group's first
@@ -365,7 +370,9 @@ static SortAhead<R> make_ahead(const cpic_grid* g, const cpic_push_params* prm, 
   a.kz = (R)(2.0 * steps * prm->cdt_dz);
   a.nx = (int)g->nx; a.ny = (int)g->ny; a.nz = (int)g->nz;
   a.sx = a.nx + 2;
-  a.sxy = a.sx * (a.ny + 2);
+  a.sy = a.ny + 2;
+  a.dsx = make_div_magic((unsigned)a.sx);
+  a.dsy = make_div_magic((unsigned)a.sy);
   return a;
 }
 

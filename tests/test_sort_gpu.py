@@ -153,8 +153,9 @@ def _ahead_keys(p, steps, cdt, nx, ny, nz, real):
     """Look-ahead keys restated in numpy with the device's operation order:
     the interior cell reached after `steps` pushes of displacement
     2 u cdt / gamma, wrapped periodically; ghost cells keep their index and
-    out-of-range cells take the last bucket.  steps = 0: the cells (a
-    particle on a +face stays in its cell)."""
+    out-of-range cells take the last bucket; the predicted offset is clamped
+    to +-(2n - 1).  steps = 0: the cells (a particle on a +face stays in its
+    cell)."""
     R = np.dtype(real).type
     sx, sy = nx + 2, ny + 2
     nc = sx * sy * (nz + 2)
@@ -171,7 +172,7 @@ def _ahead_keys(p, steps, cdt, nx, ny, nz, real):
 
         def idx(i, x, u, k, n):
             f = x + R(k) * u * rg
-            lim = R(2 * n + 1)
+            lim = R(2 * n - 1)
             f = np.where(~(f >= -lim), -lim, f)
             f = np.where(~(f <= lim), lim, f)
             shift = np.floor((f + R(1)) * R(0.5)).astype(np.int64)
