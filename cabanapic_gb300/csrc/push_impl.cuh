@@ -26,9 +26,10 @@
 //   32 * 15 * chunks_per_warp consecutive particles.  Once particles are in
 //   cell order a tile covers a short run of voxels; its cell window is a
 //   segment of wx voxels [c0, c0 + wx) around that run together with the
-//   eight segments offset by +-1 in y and z (strides sx, sx*sy): 9 segments,
-//   the cells the tile's particles reach within a sort interval except the
-//   run's ends when the run is longer than the window.  Warp 0 is a producer:
+//   segments offset by -1 and +1 in y (stride sx) and in z (stride sx*sy): 5
+//   segments, a cross, holding the cells the tile's particles reach within a
+//   sort interval except those displaced in both y and z (the diagonal rows;
+//   the 9-segment block is a build option, CPIC_TILE_WINDOW).  Warp 0 is a producer:
 //   it anchors each tile's window on the median of 32 sampled cells and stages
 //   the 18 interpolator coefficients of the window's cells in shared memory
 //   (rows of 20 values, 16-byte aligned) with cp.async, into two buffers
@@ -594,8 +595,31 @@ push_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__ inter
 }
 
 // ------------------------------------------------------------ tiled kernel
+// Shape of a tile's window, as segments of rows (y offset ky, z offset kz,
+// each 0..2 for -1, 0, +1): 9 = the 3 x 3 rows around the tile's row; 3 = the
+// tile's plane only (ky = 0..2, kz = 1); 5 = a cross, the tile's plane and the
+// tile's row in the planes above and below (the diagonal rows left out).
+// Measured at 128^3 x 64 ppc, look-ahead sort keys (mean push ms): 9 rows,
+// 7 chunks, 44 voxels 2.301-2.302; 5 rows, 7 chunks, 56 or 64 voxels
+// 2.271-2.273 (8 chunks 2.276, 6 chunks 2.298, 48 voxels 2.308); 3 rows, 7
+// chunks, 64 voxels 2.311 (fastest where the list is in cell order, slowest
+// 10 steps away from it, when a sixth of the particles sit in another plane).
+#ifndef CPIC_TILE_WINDOW
+#define CPIC_TILE_WINDOW 5
+#endif
+static_assert(CPIC_TILE_WINDOW == 9 || CPIC_TILE_WINDOW == 5 || CPIC_TILE_WINDOW == 3, "window: 9, 5 or 3 rows");
+constexpr int kWinSeg = CPIC_TILE_WINDOW;  // window segments
+
+// Segment of rows (ky, kz), or -1 if the window leaves them out.
+__device__ __forceinline__ int row_segment(int ky, int kz) {
+  if constexpr (kWinSeg == 9) return ky + 3 * kz;
+  if (kz == 1) return ky;
+  if constexpr (kWinSeg == 5) return ky == 1 ? (kz == 0 ? 3 : 4) : -1;
+  return -1;
+}
+
 // Slot of `cell` in the window, or -1.  With r = cell - c0 + sx*sy + sx the
-// window is r = dx + ky * ys + kz * zs, dx < wx <= ys, ky, kz in {0, 1, 2}.
+// rows around the tile's are r = dx + ky * ys + kz * zs, dx < wx <= ys.
 __device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, int zs) {
   int r = cell - w.c0 + ys + zs;
   if ((unsigned)r >= (unsigned)(3 * zs)) return -1;
@@ -603,12 +627,16 @@ __device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, i
   r -= kz * zs;
   const int ky = (r >= ys) + (r >= 2 * ys);
   r -= ky * ys;
-  return r < w.wx ? r + w.wx * (ky + 3 * kz) : -1;
+  const int sg = row_segment(ky, kz);
+  return (r < w.wx && sg >= 0) ? r + w.wx * sg : -1;
 }
 
-// First voxel of window segment s (ky = s % 3, kz = s / 3).
+// First voxel of window segment s.
 __device__ __forceinline__ int segment_start(const TileWin& w, int s, int ys, int zs) {
-  const int kz = s / 3, ky = s - 3 * kz;
+  int ky, kz;
+  if (kWinSeg == 9) { kz = s / 3; ky = s - 3 * kz; }
+  else if (s < 3) { ky = s; kz = 1; }
+  else { ky = 1; kz = s == 3 ? 0 : 2; }
   return w.c0 + (kz - 1) * zs + (ky - 1) * ys;
 }
 
@@ -658,7 +686,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // Window segment of slot i: s = floor(i / wx), exact in float for i < 9 * 64.
 __device__ __forceinline__ int slot_segment(int i, float inv_wx) {
-  return min((int)(((float)i + 0.5f) * inv_wx), 8);
+  return min((int)(((float)i + 0.5f) * inv_wx), kWinSeg - 1);
 }
 
 // Issues the copies of the window's interpolator rows; cells outside the
@@ -669,7 +697,7 @@ __device__ __forceinline__ int slot_segment(int i, float inv_wx) {
 template <class R>
 __device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __restrict__ interp,
                                              const TileWin w, int ys, int zs, int num_cells, int lane) {
-  const int ncell = 9 * w.wx;
+  const int ncell = kWinSeg * w.wx;
   const float inv_wx = 1.0f / (float)w.wx;
   const int q = lane & 3;
   for (int i = lane >> 2; i < ncell; i += 8) {
@@ -691,7 +719,7 @@ __device__ __forceinline__ void stage_window(R* __restrict__ buf, const R* __res
 #define CPIC_TILE_BULK 0  // stage windows with per-element cp.async (0, faster) or bulk copies (1)
 #endif
 
-// Window staging through the bulk-copy (TMA) engine.  Each of the 9 segments
+// Window staging through the bulk-copy (TMA) engine.  Each of the segments
 // of wx <= 64 voxels lies in at most 3 consecutive 32-cell AoSoA blocks of
 // the interpolator array (cell arrays hold whole blocks: cpic_cell_array_bytes);
 // lane 0 copies those blocks whole (18 x 32 values each) into one of two
@@ -786,7 +814,7 @@ __device__ __forceinline__ bool land_transpose(R* __restrict__ buf, const R* __r
   return true;
 }
 
-// Stages all 9 segments of window w into buf: segment s + 1's copy is in
+// Stages all segments of window w into buf: segment s + 1's copy is in
 // flight while segment s is transposed.  False if a wait gave up.
 template <class R>
 __device__ __forceinline__ bool stage_window_bulk(R* __restrict__ buf, R* __restrict__ land,
@@ -794,8 +822,8 @@ __device__ __forceinline__ bool stage_window_bulk(R* __restrict__ buf, R* __rest
                                                   const R* __restrict__ interp, const TileWin& w, int ys,
                                                   int zs, int nc, int lane) {
   land_issue<R>(land, lbar, ls, interp, w, 0, ys, zs, nc, lane);
-  for (int s = 0; s < 9; ++s) {
-    if (s + 1 < 9) land_issue<R>(land, lbar, ls, interp, w, s + 1, ys, zs, nc, lane);
+  for (int s = 0; s < kWinSeg; ++s) {
+    if (s + 1 < kWinSeg) land_issue<R>(land, lbar, ls, interp, w, s + 1, ys, zs, nc, lane);
     if (!land_transpose<R>(buf, land, lbar, ls, w, s, ys, zs, nc, lane)) return false;
   }
   return true;
@@ -806,7 +834,7 @@ constexpr int kConsumers = kTiledThreads / 32 - 1;  // warps 1..15 push; warp 0 
 
 template <class R>
 constexpr size_t tiled_dyn_smem(int wxmax) {
-  return (size_t)9 * wxmax * 2 * kRow * sizeof(R) + (CPIC_TILE_BULK ? 2 * kLandElems * sizeof(R) : 0);
+  return (size_t)kWinSeg * wxmax * 2 * kRow * sizeof(R) + (CPIC_TILE_BULK ? 2 * kLandElems * sizeof(R) : 0);
 }
 
 // Cell of the lane-th sample particle of tile t (tiles of T particles).
@@ -849,7 +877,7 @@ push_tiled_kernel(unsigned char* __restrict__ part, int n, const R* __restrict__
   const int nchunks = (n + 31) >> 5;
   const int ys = a.g.sx, zs = a.g.sx * a.g.sy, nc = a.g.num_cells;
   const int G = gridDim.x;
-  const size_t wrows = (size_t)9 * wxmax * kRow;
+  const size_t wrows = (size_t)kWinSeg * wxmax * kRow;
   if ((int)blockIdx.x >= ntiles) return;
   R* const land = wbuf + 2 * wrows;  // bulk staging: two landing buffers after the windows
   if (threadIdx.x == 0) {
@@ -991,19 +1019,20 @@ struct TileShape {
   int chunks_per_warp, wxmax;
 };
 
-// 7 chunks per consumer warp (3,360 particles a tile) and windows of 44 voxels
-// per segment: 2 x (62 KB window buffers + 35 KB static) per SM stays inside
-// the 196 KB shared-memory carveout, which leaves 60 KB of L1.  At 64
-// particles per cell a tile spans ~52 voxels, so its edge cells (and every
-// cell at lower densities) gather from global memory; larger tiles amortise
-// the per-tile staging and measured faster than windows that cover the
-// whole tile (4 chunks and 36 voxels: 2.55 ms, 7 and 44: 2.47 ms at 128^3 x
-// 64 ppc; 48-voxel windows cross the carveout and cost 5%).
+// 7 chunks per consumer warp (3,360 particles a tile) and cross windows of 56
+// voxels per segment: 2 x (44 KB window buffers + 35 KB static) per SM, which
+// leaves ~90 KB of L1 for the global gathers of the cells outside the window.
+// At 64 particles per cell a tile spans ~52 voxels, so the window covers it
+// once the particles are in cell order.  With 9-row windows the shared memory
+// allowed only 44 voxels (larger windows crossed the 196 KB carveout and cost
+// 5%), so a tile's edge cells gathered from global memory; larger tiles still
+// measured faster than windows covering the whole tile (4 chunks and 36
+// voxels: 2.55 ms, 7 and 44: 2.47 ms at 128^3 x 64 ppc on cell keys).
 #ifndef CPIC_TILE_CHUNKS
 #define CPIC_TILE_CHUNKS 7  // chunks per consumer warp and tile
 #endif
 #ifndef CPIC_TILE_WXMAX
-#define CPIC_TILE_WXMAX 44  // longest window segment (voxels)
+#define CPIC_TILE_WXMAX 56  // longest window segment (voxels)
 #endif
 static_assert(CPIC_TILE_WXMAX <= 64, "a window segment must fit the 3-block landing buffers");
 inline TileShape tile_shape(const GridDev& g) {
