@@ -83,7 +83,8 @@ struct PushArgs {
 };
 
 // Cell window of one tile: segments [c0 + off_s, c0 + off_s + wx) with
-// off_s = (s / 3 - 1) * sx * sy + (s % 3 - 1) * sx, s = 0..8.
+// off_s = (kz - 1) * sx * sy + (ky - 1) * sx for the rows (ky, kz) of the
+// window's shape (segment_start).
 struct TileWin {
   int c0, wx;
 };
@@ -444,7 +445,7 @@ struct LaneCtx {
   unsigned lt_mask;
 };
 
-__device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, int zs);
+__host__ __device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, int zs);
 
 // One 32-particle chunk: gather, Boris, in-cell move and deposit, queueing of
 // the crossers.  TILED gathers from the shared-memory window `wbuf` when the
@@ -611,7 +612,7 @@ static_assert(CPIC_TILE_WINDOW == 9 || CPIC_TILE_WINDOW == 5 || CPIC_TILE_WINDOW
 constexpr int kWinSeg = CPIC_TILE_WINDOW;  // window segments
 
 // Segment of rows (ky, kz), or -1 if the window leaves them out.
-__device__ __forceinline__ int row_segment(int ky, int kz) {
+__host__ __device__ __forceinline__ int row_segment(int ky, int kz) {
   if constexpr (kWinSeg == 9) return ky + 3 * kz;
   if (kz == 1) return ky;
   if constexpr (kWinSeg == 5) return ky == 1 ? (kz == 0 ? 3 : 4) : -1;
@@ -620,7 +621,7 @@ __device__ __forceinline__ int row_segment(int ky, int kz) {
 
 // Slot of `cell` in the window, or -1.  With r = cell - c0 + sx*sy + sx the
 // rows around the tile's are r = dx + ky * ys + kz * zs, dx < wx <= ys.
-__device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, int zs) {
+__host__ __device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, int zs) {
   int r = cell - w.c0 + ys + zs;
   if ((unsigned)r >= (unsigned)(3 * zs)) return -1;
   const int kz = (r >= zs) + (r >= 2 * zs);
@@ -632,7 +633,7 @@ __device__ __forceinline__ int window_slot(int cell, const TileWin& w, int ys, i
 }
 
 // First voxel of window segment s.
-__device__ __forceinline__ int segment_start(const TileWin& w, int s, int ys, int zs) {
+__host__ __device__ __forceinline__ int segment_start(const TileWin& w, int s, int ys, int zs) {
   int ky, kz;
   if (kWinSeg == 9) { kz = s / 3; ky = s - 3 * kz; }
   else if (s < 3) { ky = s; kz = 1; }
