@@ -235,6 +235,17 @@ class Simulation:
         order of the accumulator sums differs from upload, run, download."""
         if steps < 1:
             raise ValueError("steps must be >= 1")
+        nbytes = self.particles.nbytes
+        for name, t in (("pinned_in", pinned_in), ("pinned_out", pinned_out)):
+            if t is None:
+                continue
+            if t.dtype != torch.uint8 or t.device.type != "cpu" or not t.is_pinned() or t.numel() < nbytes:
+                raise ValueError(f"{name}: a pinned host uint8 tensor of at least {nbytes} bytes")
+        if pinned_in is None:
+            raise ValueError("pinned_in is required")
+        if energies_out is not None and (energies_out.device.type != "cpu" or tuple(energies_out.shape[1:]) != (2,)
+                                         or energies_out.shape[0] < steps):
+            raise ValueError("energies_out: a host tensor of shape [steps, 2]")
         dev = self.particles.buf.device
         cur = torch.cuda.current_stream(dev)
         runs = block_pieces(self.particles.n, self.particles.vl, pieces)

@@ -39,3 +39,20 @@ def test_particle_list_view_shares_memory_and_checks_alignment():
     for start, count in ((16, 10), (-32, 10), (64, 40), (0, -1)):
         with pytest.raises(ValueError):
             P.view(start, count)
+
+
+def test_run_from_host_rejects_unsuitable_host_buffers():
+    """Simulation.run_from_host checks its host buffers before any copy: a
+    pinned uint8 tensor of the list's size in, likewise out, energies [steps, 2]."""
+    from types import SimpleNamespace
+    from cabanapic_gb300.simulation import Simulation
+    fake = SimpleNamespace(particles=SimpleNamespace(nbytes=4096))
+    ok_size = torch.zeros(4096, dtype=torch.uint8)  # not pinned (no GPU here)
+    with pytest.raises(ValueError):
+        Simulation.run_from_host(fake, ok_size, 3)
+    with pytest.raises(ValueError):
+        Simulation.run_from_host(fake, torch.zeros(1024, dtype=torch.float32), 3)
+    with pytest.raises(ValueError):
+        Simulation.run_from_host(fake, None, 3)
+    with pytest.raises(ValueError):
+        Simulation.run_from_host(fake, ok_size, 0)
