@@ -56,3 +56,28 @@ def test_run_from_host_rejects_unsuitable_host_buffers():
         Simulation.run_from_host(fake, None, 3)
     with pytest.raises(ValueError):
         Simulation.run_from_host(fake, ok_size, 0)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cabanapic_gb300 import build, capi
+    build.build()
+    return capi.load()
+
+
+def test_sorter_look_ahead_arguments(lib):
+    """pic.Sorter takes look-ahead keys only double-buffered and with the grid
+    and the cdt's; negative look-ahead is refused."""
+    from cabanapic_gb300.arrays import ParticleList
+    from cabanapic_gb300 import pic
+    P = ParticleList(64, np.float32, 32, device="cpu")
+    ahead = ((4, 4, 4), (0.4, 0.4, 0.4))
+    with pytest.raises(ValueError):
+        pic.Sorter(P, 216, double_buffer=False, steps_ahead=5, ahead=ahead)
+    with pytest.raises(ValueError):
+        pic.Sorter(P, 216, double_buffer=True, steps_ahead=5)
+    with pytest.raises(ValueError):
+        pic.Sorter(P, 216, double_buffer=True, steps_ahead=-1, ahead=ahead)
+    s = pic.Sorter(P, 216, double_buffer=True, steps_ahead=5, ahead=ahead)
+    assert s.steps_ahead == 5 and s._prm.precision == 4 and s._prm.particle_vl == 32
+    assert abs(s._prm.cdt_dx - 0.4) < 1e-12 and s._grid.nx == 4
