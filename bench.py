@@ -3,7 +3,9 @@
 Workload (the reference's throughput configuration): uniform thermal plasma,
 128^3 periodic cells, 64 electrons per cell (134,217,728 particles), FP32,
 u_th = 0.05, dt = 0.7 Courant, zero initial fields, particles re-sorted by
-cell every 20 steps.  A "step" is the reference's whole time step
+cell every 20 steps (keyed by the cell each particle reaches 10 pushes later,
+so that the list is in cell order midway between sorts; any order is a valid
+list).  A "step" is the reference's whole time step
 (example/example.cpp:221-271): interpolator load, accumulator clear, push with
 deposit, accumulator unload, B half step, E step, B half step, field energies,
 plus the amortised sort.  The particle list (4.3 GB) is larger than L2, so no
@@ -14,7 +16,8 @@ L2 flush is needed between steps.
 Prints one JSON line.  `value` is pushes/s with the state resident in HBM;
 `e2e` is the same metric through the public API with the initial state copied
 from pinned host memory and the final state copied back inside the timed
-region (plus each step's energies read back); `roofline` covers the push
+region (plus each step's energies read back; median of five timed runs);
+`e2e_cpp` the same through the C++ push() interface; `roofline` covers the push
 kernel; `cpu_baseline` is the CPU restatement (OpenMP, all host cores) on a
 bounded sample of the same workload.  `--impl reference` times that CPU
 implementation as the reference arm (the reference itself needs Kokkos and
